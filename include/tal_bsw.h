@@ -1,0 +1,120 @@
+/*
+ * tal_bsw.h -- C ABI of the GB300 banded Smith-Waterman seed extension.
+ *
+ * Drop-in replacement for TAL's BandedPairWiseSW (src/alignment/BSW/bandedSWA.h)
+ * on one GB300 GPU (sm_103a).  Plain C types only: pointers, sizes, status codes.
+ *
+ * Semantics follow the reference's inter-task SIMD kernels getScores16 /
+ * getScores8 (bandedSWA.cpp:2664-3356 / :1970-2661) bit for bit:
+ *   target  seq1 = seqBufRef + idr, length len1   (bandedSWA.cpp:2806)
+ *   query   seq2 = seqBufQer + idq, length len2   (bandedSWA.cpp:2848)
+ *   bases 0..3, 4 = N; outputs score, tle, gtle, qle, gscore, max_off are
+ *   written into the caller's SeqPair records, [0, numPairs) only.
+ */
+#ifndef TAL_BSW_H
+#define TAL_BSW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference's functions return void and exit() or assert()
+ * on failure (bandedSWA.cpp:88-93, 2705-2708); every entry point here returns
+ * one of these instead. */
+enum {
+    TAL_OK = 0,
+    TAL_EINVAL = 1,   /* bad argument: NULL pointer, negative count, bad bits */
+    TAL_EDOMAIN = 2,  /* a pair outside the kernel's exact range (see below) */
+    TAL_ENOMEM = 3,   /* device or pinned-host allocation failed */
+    TAL_ECUDA = 4,    /* a CUDA runtime call failed */
+    TAL_ETIMEOUT = 5, /* a bounded wait ran out */
+    TAL_ENODEV = 6,   /* no usable sm_103 device */
+    TAL_EBUSY = 7     /* serving queue full / handle in use */
+};
+
+/* Precision selector for tal_bsw_scores*. */
+enum {
+    TAL_BSW_AUTO = 0, /* per pair: 8-bit rules where eligible, else 16-bit */
+    TAL_BSW_8 = 8,    /* getScores8  (bandedSWA.h:257-262) */
+    TAL_BSW_16 = 16   /* getScores16 (bandedSWA.h:285-290) */
+};
+
+/* SeqPair, bandedSWA.h:90-99: 14 x int32 = 56 bytes, fields in this order. */
+typedef struct tal_seq_pair {
+    int32_t idr, idq, id;
+    int32_t len1, len2;
+    int32_t h0;
+    int32_t seqid, regid;
+    int32_t score, tle, gtle, qle;
+    int32_t gscore, max_off;
+} tal_seq_pair;
+
+/* Constructor arguments of BandedPairWiseSW (bandedSWA.h:118-121).  The
+ * reference's vector kernels ignore its scoring matrix and score a match
+ * with w_match, a mismatch with -w_mismatch and any N with -1
+ * (bandedSWA.cpp:64-68, 1883-1892); so does this library. */
+typedef struct tal_bsw_params {
+    int32_t o_del, e_del, o_ins, e_ins;
+    int32_t zdrop, end_bonus;
+    int32_t w_match;    /* a  (int8 in the reference) */
+    int32_t w_mismatch; /* b, positive penalty (int8 in the reference) */
+} tal_bsw_params;
+
+typedef struct tal_bsw_ctx *tal_bsw_handle;
+
+/* Replaces BandedPairWiseSW::BandedPairWiseSW (bandedSWA.cpp:50-94).  Binds
+ * the calling thread's current device (or `device` if >= 0), creates a stream
+ * and grow-only device buffers.  Parameters outside the exact range
+ * (0 <= o <= 127, 1 <= e <= 127, 0 <= a, b <= 127) give TAL_EINVAL. */
+int tal_bsw_create(const tal_bsw_params *params, int device, tal_bsw_handle *out);
+
+/* Replaces ~BandedPairWiseSW (bandedSWA.cpp:97-100). */
+int tal_bsw_destroy(tal_bsw_handle h);
+
+/* Replaces getScores8 / getScores16 (bandedSWA.cpp:1970, 2664) on host
+ * buffers: copies the pairs and the byte ranges they reference to the
+ * device, scores them, and writes the six outputs back into pairs[0, n).
+ * bits: TAL_BSW_8, TAL_BSW_16 or TAL_BSW_AUTO.  w: band, per call.
+ *
+ * Exact range: 16-bit needs len1, len2 <= 32767, h0 >= 0 and
+ * h0 + w_match * min(len1, len2) <= 32767; 8-bit needs len1, len2 <= 127 and
+ * h0 + w_match * min(len1, len2) <= 127 (the reference's own 8-bit limits,
+ * bandedSWA.h:82 and the int8 score range) plus two no-wrap conditions on
+ * the first column and the gap scores.  A pair outside it gives TAL_EDOMAIN
+ * (for AUTO: outside both), and no outputs are written. */
+int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufRef,
+                   const uint8_t *seqBufQer, int32_t numPairs, int32_t w, int bits);
+
+/* The same on device-resident buffers (cudaMalloc'd), asynchronous on the
+ * handle's stream; d_w, if not NULL, gives a band per pair instead of w.
+ * ref_bytes / qer_bytes are the allocation sizes of d_ref / d_qer (reads stay
+ * inside them).  Call tal_bsw_sync to wait and collect the status. */
+int tal_bsw_scores_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t *d_ref,
+                          size_t ref_bytes, const uint8_t *d_qer, size_t qer_bytes,
+                          int32_t numPairs, int32_t w, const int32_t *d_w, int bits);
+
+/* Waits for the handle's stream; returns the first error any launch on it
+ * reported since the last sync. */
+int tal_bsw_sync(tal_bsw_handle h);
+
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their
+ * own copies against the scorer. */
+void *tal_bsw_stream(tal_bsw_handle h);
+
+/* Human-readable text of the last error on this handle ("" if none). */
+const char *tal_bsw_last_error(tal_bsw_handle h);
+
+/* Index of the first pair that gave TAL_EDOMAIN in the last call, or -1. */
+int64_t tal_bsw_last_bad_pair(tal_bsw_handle h);
+
+/* Number of kernel launches this handle has issued (for accounting). */
+uint64_t tal_bsw_launch_count(tal_bsw_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TAL_BSW_H */

@@ -1,0 +1,171 @@
+"""ORACLE — test infrastructure only.
+
+ctypes front end for the CPU restatement of the reference's banded
+Smith-Waterman (oracle/bsw_oracle.cpp, built into oracle/_build/) and, where it
+was built on this machine, for the reference itself (oracle/_ref/, built from
+the reference sources by oracle/build_ref.sh).  Only tests/, the smoke check
+and bench.py's CPU legs import this package; the product library never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Dict, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle_bsw.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+_PARAM_KEYS = ("o_del", "e_del", "o_ins", "e_ins", "zdrop", "end_bonus", "a", "b")
+_libs: Dict[str, ctypes.CDLL] = {}
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement (g++, host only)."""
+    src = os.path.join(HERE, "bsw_oracle.cpp")
+    if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
+        os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
+        subprocess.check_call(["g++", "-O3", "-fPIC", "-shared", "-pthread", "-o", ORACLE_SO, src])
+    return ORACLE_SO
+
+
+def build_ref() -> None:
+    """Compile the reference from its own sources into oracle/_ref (x86 only;
+    a no-op where the reference tree is absent)."""
+    subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")])
+
+
+def _oracle():
+    if "oracle" not in _libs:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        lib = ctypes.CDLL(ORACLE_SO)
+        lib.oracle_bsw_vector.restype = ctypes.c_int
+        lib.oracle_bsw_vector.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_int32, ctypes.c_int]
+        lib.oracle_bsw_scalar.restype = ctypes.c_int
+        lib.oracle_bsw_scalar.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                          ctypes.c_void_p, ctypes.c_int]
+        _libs["oracle"] = lib
+    return _libs["oracle"]
+
+
+def _params(p: Dict[str, int]) -> np.ndarray:
+    return np.array([int(p[k]) for k in _PARAM_KEYS], np.int32)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def vector(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w: int,
+           params: Dict[str, int], bits: int = 16, lanes: Optional[int] = None,
+           nthreads: int = 1) -> np.ndarray:
+    """getScores16 / getScores8 restated; returns a scored copy of ``pairs``.
+    lanes: group width (default 32 for 16-bit, 64 for 8-bit, as the reference)."""
+    out = np.ascontiguousarray(pairs).copy()
+    lanes = lanes or (32 if bits == 16 else 64)
+    pv = _params(params)
+    rc = _oracle().oracle_bsw_vector(_ptr(pv), bits, lanes, _ptr(out), out.shape[0],
+                                     _ptr(ref), _ptr(qer), int(w), nthreads)
+    if rc != 0:
+        raise ValueError("oracle_bsw_vector rejected its arguments")
+    return out
+
+
+def scalar(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w: int,
+           params: Dict[str, int], nthreads: int = 1):
+    """scalarBandedSWAWrapper restated; returns (scored copy, ref-cells)."""
+    out = np.ascontiguousarray(pairs).copy()
+    pv = _params(params)
+    cells = np.zeros(1, np.uint64)
+    rc = _oracle().oracle_bsw_scalar(_ptr(pv), _ptr(out), out.shape[0], _ptr(ref), _ptr(qer),
+                                     int(w), _ptr(cells), nthreads)
+    if rc != 0:
+        raise ValueError("oracle_bsw_scalar rejected its arguments")
+    return out, int(cells[0])
+
+
+def ref_available(isa: str = "avx512") -> bool:
+    return os.path.exists(os.path.join(REF_DIR, f"libbsw_ref_{isa}.so"))
+
+
+def reference(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w: int,
+              params: Dict[str, int], mode: int = 16, isa: str = "avx512",
+              pristine: bool = True) -> np.ndarray:
+    """The reference's own getScores16 (mode 16) / getScores8 (8) /
+    scalarBandedSWAWrapper (0), compiled from its sources.
+
+    pristine: run the vector kernels one SIMD group at a time on zeroed
+    scratch rows, which makes them deterministic (the reference reads one
+    scratch cell per group that it may not have written; see ref_shim.cpp)."""
+    key = "ref_" + isa
+    if key not in _libs:
+        path = os.path.join(REF_DIR, f"libbsw_ref_{isa}.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"reference build missing: {path}")
+        lib = ctypes.CDLL(path)
+        lib.ref_bsw_run.restype = ctypes.c_int
+        lib.ref_bsw_run.argtypes = [ctypes.c_int] * 9 + [ctypes.c_void_p, ctypes.c_void_p,
+                                                         ctypes.c_void_p, ctypes.c_int32,
+                                                         ctypes.c_int32, ctypes.c_int]
+        _libs[key] = lib
+    lib = _libs[key]
+    out = np.ascontiguousarray(pairs).copy()
+    p = params
+    rc = lib.ref_bsw_run(p["o_del"], p["e_del"], p["o_ins"], p["e_ins"], p["zdrop"],
+                         p["end_bonus"], p["a"], p["b"], mode, _ptr(out), _ptr(ref), _ptr(qer),
+                         out.shape[0], int(w), 1 if pristine else 0)
+    if rc != 0:
+        raise RuntimeError("ref_bsw_run failed")
+    return out
+
+
+def eligible8(pairs: np.ndarray, w, params: Dict[str, int]) -> np.ndarray:
+    """Per-pair 8-bit eligibility: the reference's own 8-bit limits
+    (len1, len2 < MAX_SEQ_LEN8 = 128, bandedSWA.h:82; h0 + a*min(len1, len2) in
+    int8 range) plus the no-wrap conditions under which getScores8 and an
+    exact-integer evaluation agree (gap scores and the first column in int8)."""
+    p = params
+    l1 = pairs["len1"].astype(np.int64)
+    l2 = pairs["len2"].astype(np.int64)
+    h0 = pairs["h0"].astype(np.int64)
+    w = np.broadcast_to(np.asarray(w, np.int64), l1.shape)
+    ok = (l1 >= 0) & (l2 >= 0) & (l1 <= 127) & (l2 <= 127) & (h0 >= 0)
+    ok &= h0 + p["a"] * np.minimum(l1, l2) <= 127
+    oe = max(p["o_del"] + p["e_del"], p["o_ins"] + p["e_ins"])
+    if oe > 127 or 1 - max(p["b"], 1) - oe < -128:
+        return np.zeros(l1.shape, bool)
+    kmax = np.minimum(l1 - 1, np.maximum(w, 0) + 1)
+    ok &= (kmax < 1) | (h0 - p["o_del"] - kmax * p["e_del"] >= -128)
+    return ok
+
+
+def routed(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w, params: Dict[str, int],
+           bits: int = 0, nthreads: int = 1) -> np.ndarray:
+    """Scores every pair with getScores8 or getScores16 semantics: bits 8/16
+    forces one; bits 0 routes each pair by eligible8().  w may be a scalar or
+    a per-pair array (pairs are grouped by band; results do not depend on
+    grouping)."""
+    out = np.ascontiguousarray(pairs).copy()
+    n = out.shape[0]
+    if n == 0:
+        return out
+    warr = np.broadcast_to(np.asarray(w, np.int64), (n,))
+    if bits == 8:
+        is8 = np.ones(n, bool)
+    elif bits == 16:
+        is8 = np.zeros(n, bool)
+    else:
+        is8 = eligible8(out, warr, params)
+    for wv in np.unique(warr):
+        for b in (8, 16):
+            sel = np.nonzero((warr == wv) & (is8 == (b == 8)))[0]
+            if sel.size:
+                out[sel] = vector(out[sel], ref, qer, int(wv), params, bits=b, nthreads=nthreads)
+    return out

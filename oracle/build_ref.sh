@@ -1,0 +1,32 @@
+#!/usr/bin/env bash
+# Builds the reference's own banded Smith-Waterman (bandedSWA.cpp) from the
+# read-only reference tree into oracle/_ref/, for pinning the oracle and for
+# generating golden fixtures.  Test infrastructure only.
+#
+# The reference header includes "macro.h", which the reference tree does not
+# ship; an empty stub stands in for it.  x86-64 only: the kernels under test are
+# the AVX-512BW (and AVX2) paths.  On any other host this script does nothing.
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF_BSW="${TAL_REFERENCE_ROOT:-/root/reference}/src/alignment/BSW"
+OUT="$HERE/_ref"
+if [ ! -f "$REF_BSW/bandedSWA.cpp" ]; then
+  echo "build_ref: reference sources not present; skipping" >&2
+  exit 0
+fi
+case "$(uname -m)" in
+  x86_64) ;;
+  *) echo "build_ref: reference SIMD paths are x86-only; skipping" >&2; exit 0 ;;
+esac
+mkdir -p "$OUT/stub"
+: > "$OUT/stub/macro.h"
+build() {  # $1 = isa flag, $2 = suffix
+  g++ -O2 -fPIC -shared $1 -w -I"$OUT/stub" -I"$REF_BSW" \
+      "$REF_BSW/bandedSWA.cpp" "$HERE/ref_shim.cpp" -o "$OUT/libbsw_ref_$2.so"
+}
+if grep -q avx512bw /proc/cpuinfo; then
+  build -mavx512bw avx512 &
+fi
+build -mavx2 avx2 &
+wait
+ls "$OUT"/*.so

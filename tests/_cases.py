@@ -1,0 +1,115 @@
+"""Seeded pair sets shared by the CPU and GPU tests: the workload shapes at
+test sizes, and edge cases of the kinds the reference's code paths branch on
+(empty and one-base sequences, N-rich input, h0 at the range limits, z-drop
+firing mid-band, end_bonus moving the band, zero rows, narrow bands, the 8-bit
+envelope edges, gap extension != 1)."""
+import numpy as np
+
+from tal_bsw import synth
+from tal_bsw.seqpair import new_pairs
+
+DEFAULT = dict(o_del=6, e_del=1, o_ins=6, e_ins=1, zdrop=100, end_bonus=5, a=1, b=4)
+
+
+def pack(seqs_ref, seqs_qer, h0s, slack=64):
+    n = len(seqs_ref)
+    p = new_pairs(n)
+    l1 = np.array([len(s) for s in seqs_ref], np.int64)
+    l2 = np.array([len(s) for s in seqs_qer], np.int64)
+    ro = np.concatenate([[0], np.cumsum(l1)[:-1]]) if n else np.zeros(0, np.int64)
+    qo = np.concatenate([[0], np.cumsum(l2)[:-1]]) if n else np.zeros(0, np.int64)
+    p["len1"], p["len2"], p["h0"] = l1, l2, np.asarray(h0s, np.int64)
+    p["idr"], p["idq"] = ro, qo
+    p["id"] = np.arange(n)
+    ref = np.concatenate([np.asarray(s, np.uint8) for s in seqs_ref] + [np.zeros(slack, np.uint8)])
+    qer = np.concatenate([np.asarray(s, np.uint8) for s in seqs_qer] + [np.zeros(slack, np.uint8)])
+    return p, ref, qer
+
+
+def mutate(rng, q, div, nrate=0.0):
+    r = q.copy()
+    m = rng.random(len(r)) < div
+    r[m] = rng.integers(0, 4, int(m.sum()))
+    if nrate:
+        r[rng.random(len(r)) < nrate] = 4
+    return r
+
+
+def edge_cases(seed=7, bits=16):
+    """(name, pairs, ref, qer, w, params) tuples."""
+    rng = np.random.default_rng(seed)
+    lmax = 127 if bits == 8 else 400
+    out = []
+
+    def add(name, refs, qers, h0s, w=100, **kw):
+        P = dict(DEFAULT)
+        P.update(kw)
+        p, r, q = pack(refs, qers, h0s)
+        out.append((name, p, r, q, w, P))
+
+    # empty and one-base sequences
+    refs, qers, h0s = [], [], []
+    for l1 in (0, 1, 2):
+        for l2 in (0, 1, 2):
+            for h0 in (0, 1, 7, 30):
+                refs.append(rng.integers(0, 4, l1)); qers.append(rng.integers(0, 4, l2)); h0s.append(h0)
+    add("tiny", refs, qers, h0s)
+    # N-rich sequences
+    refs, qers, h0s = [], [], []
+    for _ in range(64):
+        l2 = int(rng.integers(1, min(lmax, 120)))
+        q = rng.integers(0, 4, l2).astype(np.uint8)
+        q[rng.random(l2) < 0.3] = 4
+        r = mutate(rng, q, 0.05, nrate=0.2)[: min(lmax, l2 + int(rng.integers(0, 8)))]
+        refs.append(r); qers.append(q); h0s.append(int(rng.integers(0, 40)))
+    add("n_rich", refs, qers, h0s)
+    # h0 at range limits (8-bit: h0 + min(len) = 127)
+    refs, qers, h0s = [], [], []
+    for _ in range(64):
+        l2 = int(rng.integers(1, 100)); l1 = min(lmax, l2 + int(rng.integers(0, 20)))
+        q = rng.integers(0, 4, l2).astype(np.uint8)
+        r = np.concatenate([mutate(rng, q, 0.02), rng.integers(0, 4, max(0, l1 - l2))])[:l1]
+        h0 = 127 - min(l1, l2) if bits == 8 else int(rng.choice([0, 1, 200, 1000]))
+        refs.append(r); qers.append(q); h0s.append(max(h0, 0))
+    add("h0_limits", refs, qers, h0s)
+    # random (unrelated) sequences: zero rows early, z-drop
+    refs, qers, h0s = [], [], []
+    for _ in range(96):
+        l1 = int(rng.integers(1, lmax)); l2 = int(rng.integers(1, lmax))
+        refs.append(rng.integers(0, 4, l1)); qers.append(rng.integers(0, 4, l2)); h0s.append(int(rng.integers(0, 25)))
+    add("unrelated", refs, qers, h0s)
+    # similar then diverging: z-drop mid-band
+    refs, qers, h0s = [], [], []
+    for _ in range(96):
+        l2 = int(rng.integers(30, lmax)); cut = int(rng.integers(5, l2))
+        q = rng.integers(0, 4, l2).astype(np.uint8)
+        r = np.concatenate([q[:cut], rng.integers(0, 4, l2 - cut)]).astype(np.uint8)[:lmax]
+        refs.append(r); qers.append(q); h0s.append(int(rng.integers(5, 60)) if bits == 16 else 5)
+    for zd in (0, 1, 5, 20):
+        add(f"zdrop_{zd}", refs, qers, h0s, zdrop=zd)
+    # narrow and tiny bands, band wider than the sequences
+    refs, qers, h0s = [], [], []
+    for _ in range(64):
+        l2 = int(rng.integers(5, lmax)); l1 = int(rng.integers(5, lmax))
+        q = rng.integers(0, 4, l2).astype(np.uint8)
+        r = np.concatenate([mutate(rng, q, 0.05), rng.integers(0, 4, 200)])[:l1]
+        refs.append(r); qers.append(q); h0s.append(int(rng.integers(0, 30)))
+    for w in (0, 1, 3, 17, 500):
+        add(f"band_{w}", refs, qers, h0s, w=w)
+    # end_bonus moving the band clamp, gap extension != 1, other scores
+    add("end_bonus_0", refs, qers, h0s, w=50, end_bonus=0)
+    add("end_bonus_40", refs, qers, h0s, w=50, end_bonus=40)
+    add("gap_e2", refs, qers, h0s, w=30, e_del=2, e_ins=2, o_del=4, o_ins=3)
+    add("gap_asym", refs, qers, h0s, w=30, e_del=1, e_ins=3, o_del=9, o_ins=2)
+    add("match2", refs, qers, [min(h, 10) for h in h0s], w=40, a=2, b=3) if bits == 16 else None
+    return [c for c in out if c is not None]
+
+
+def workload_slices(n_scale=1.0):
+    """(name, Batch, bits) for every workload shape at test size."""
+    sizes = {"c1_151bp": 600, "c1_8bit": 600, "c2_16bit": 600, "c3_mixed": 1200, "c4_long": 24}
+    res = []
+    for name, n in sizes.items():
+        wl = synth.WORKLOADS[name]
+        res.append((name, synth.generate(wl, max(1, int(n * n_scale))), wl.bits))
+    return res

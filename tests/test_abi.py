@@ -1,0 +1,62 @@
+"""The C-ABI library loads and exports every function include/*.h declares;
+SeqPair keeps the reference's 56-byte layout.  No compute calls (CPU only)."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+
+import tal_bsw
+from tal_bsw.seqpair import SEQPAIR_DTYPE, SEQPAIR_FIELDS
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(tal_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_entry_points():
+    names = _declared()
+    for must in ("tal_bsw_create", "tal_bsw_destroy", "tal_bsw_scores", "tal_bsw_scores_device",
+                 "tal_bsw_last_error"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(tal_bsw.CORE_LIB)
+    missing = [n for n in _declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_seqpair_layout():
+    assert SEQPAIR_DTYPE.itemsize == 56
+    assert list(SEQPAIR_DTYPE.names) == list(SEQPAIR_FIELDS)
+    assert [SEQPAIR_DTYPE.fields[f][1] for f in SEQPAIR_FIELDS] == list(range(0, 56, 4))
+
+
+def test_create_without_gpu_fails_cleanly():
+    """On a machine without a GB300 the constructor raises (no CPU fallback)."""
+    import torch
+    if torch.cuda.is_available():
+        return
+    try:
+        tal_bsw.BandedPairWiseSW(6, 1, 6, 1, 100, 5, None, 1, 4, 1)
+    except tal_bsw.TalBswError as e:
+        assert e.status == tal_bsw.api.TAL_ENODEV
+    else:
+        raise AssertionError("expected TAL_ENODEV")
+
+
+def test_bad_params_rejected_before_device():
+    lib = tal_bsw.api.core_lib()
+    p = tal_bsw.api._Params(6, 0, 6, 1, 100, 5, 1, 4)   # e_del = 0
+    h = ctypes.c_void_p()
+    assert lib.tal_bsw_create(ctypes.byref(p), 0, ctypes.byref(h)) == tal_bsw.api.TAL_EINVAL

@@ -1,0 +1,102 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on the same
+seeded inputs -- every workload shape at test size, the edge cases, and the
+golden fixtures the reference itself produced.  Integer outputs: bit-exact."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import tal_bsw
+from tal_bsw import synth
+from tal_bsw.seqpair import outputs
+
+from _cases import edge_cases, workload_slices
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _bsw(P):
+    return tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                    P["end_bonus"], None, P["a"], P["b"], 1, device=0)
+
+
+def _gpu(pairs, ref, qer, w, P, bits):
+    got = pairs.copy()
+    with _bsw(P) as bsw:
+        if np.ndim(w) == 0:
+            bsw._scores(got, ref, qer, got.shape[0], int(w), bits)
+        else:  # per-pair band: one call per band value (the reference's w is per call)
+            for wv in np.unique(w):
+                sel = np.nonzero(w == wv)[0]
+                sub = got[sel].copy()
+                bsw._scores(sub, ref, qer, sub.shape[0], int(wv), bits)
+                got[sel] = sub
+    return got
+
+
+def _assert_same(exp, got, what):
+    e, g = outputs(exp), outputs(got)
+    bad = np.nonzero((e != g).any(axis=1))[0]
+    if bad.size:
+        k = int(bad[0])
+        raise AssertionError(
+            f"{what}: {bad.size}/{len(e)} pairs differ; first #{k} "
+            f"(len1={exp['len1'][k]} len2={exp['len2'][k]} h0={exp['h0'][k]}): "
+            f"gpu {g[k].tolist()} oracle {e[k].tolist()} "
+            "(score, tle, gtle, qle, gscore, max_off)")
+
+
+@pytest.mark.parametrize("case", workload_slices(), ids=lambda c: c[0])
+def test_workload_shapes(case):
+    name, b, bits = case
+    P = b.workload.params()
+    w = b.w if b.workload.w_choices else b.workload.w
+    exp = oracle.routed(b.pairs, b.ref, b.qer, w, P, bits=bits)
+    got = _gpu(b.pairs, b.ref, b.qer, w, P, bits)
+    _assert_same(exp, got, name)
+
+
+@pytest.mark.parametrize("bits", [16, 8])
+def test_edge_cases(bits):
+    for name, p, r, q, w, P in edge_cases(bits=bits):
+        if bits == 8:
+            keep = oracle.eligible8(p, w, P)
+            p = p[keep]
+            if p.shape[0] == 0:
+                continue
+        exp = oracle.vector(p, r, q, w, P, bits=bits)
+        got = _gpu(p, r, q, w, P, bits)
+        _assert_same(exp, got, f"{name}/{bits}")
+
+
+def test_golden_fixtures():
+    files = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+    assert files, "no golden fixtures"
+    for f in files:
+        d = np.load(f)
+        P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+        got = _gpu(d["inputs"], d["ref"], d["qer"], d["w"], P, int(d["bits"]))
+        _assert_same(d["expected"], got, os.path.basename(f))
+
+
+def test_auto_routing_matches_forced():
+    b = synth.generate(synth.C1_8, 500)
+    P = b.workload.params()
+    a = _gpu(b.pairs, b.ref, b.qer, 100, P, 0)
+    e8 = _gpu(b.pairs, b.ref, b.qer, 100, P, 8)
+    _assert_same(e8, a, "auto vs 8-bit on 8-bit-eligible pairs")
+
+
+def test_out_of_range_rejected():
+    b = synth.generate(synth.C1, 64)   # 151 bp: outside the 8-bit range
+    P = b.workload.params()
+    got = b.pairs.copy()
+    with _bsw(P) as bsw:
+        with pytest.raises(tal_bsw.TalBswError) as ei:
+            bsw.getScores8(got, b.ref, b.qer, b.n, 1, 100)
+        assert ei.value.status == tal_bsw.api.TAL_EDOMAIN
+        assert ei.value.bad_pair == 0
+    assert (outputs(got) == -1).all(), "no outputs are written on a range error"

@@ -1,0 +1,102 @@
+"""Pins the oracle (CPU restatement) to the reference: the golden fixtures
+produced by the reference itself, and -- where the reference was compiled in
+this container -- fresh seeded comparisons.  Also checks the property the GPU
+design relies on: a pair's outputs do not depend on its SIMD group."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tal_bsw import synth
+from tal_bsw.seqpair import outputs
+
+from _cases import edge_cases
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FILES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def _load(f):
+    d = np.load(f)
+    P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+    return d, P
+
+
+def test_fixtures_present():
+    assert len(FILES) >= 30
+
+
+@pytest.mark.parametrize("f", FILES, ids=os.path.basename)
+def test_oracle_matches_golden(f):
+    d, P = _load(f)
+    got = oracle.routed(d["inputs"], d["ref"], d["qer"], d["w"], P, bits=int(d["bits"]))
+    e, g = outputs(d["expected"]), outputs(got)
+    assert (e == g).all(), f"{(e != g).any(1).sum()} pairs differ"
+
+
+@pytest.mark.parametrize("f", [f for f in FILES if "wl_" in f or "zdrop" in f], ids=os.path.basename)
+def test_group_invariance(f):
+    """Pair-at-a-time (1 lane) equals the reference's 32/64-lane grouping and a
+    reversed order (so other group compositions)."""
+    d, P = _load(f)
+    bits = int(d["bits"])
+    if bits == 0 or np.ndim(d["w"]) != 0:
+        pytest.skip("mixed routing / per-pair band: covered by the golden comparison")
+    p = d["inputs"]
+    one = oracle.vector(p, d["ref"], d["qer"], int(d["w"]), P, bits=bits, lanes=1)
+    rev = oracle.vector(p[::-1].copy(), d["ref"], d["qer"], int(d["w"]), P, bits=bits)[::-1]
+    assert (outputs(one) == outputs(d["expected"])).all()
+    assert (outputs(rev) == outputs(d["expected"])).all()
+
+
+needs_ref = pytest.mark.skipif(not oracle.ref_available(), reason="reference not compiled here")
+
+
+@needs_ref
+@pytest.mark.parametrize("name", ["c1_151bp", "c1_8bit", "c2_16bit"])
+def test_oracle_vs_reference_fresh(name):
+    wl = synth.WORKLOADS[name]
+    b = synth.generate(wl.scaled(3000, seed=wl.seed + 1000))
+    bits = 8 if wl.bits == 8 else 16
+    r = oracle.reference(b.pairs, b.ref, b.qer, wl.w, wl.params(), mode=bits)
+    o = oracle.vector(b.pairs, b.ref, b.qer, wl.w, wl.params(), bits=bits, nthreads=4)
+    assert (outputs(r) == outputs(o)).all()
+
+
+@needs_ref
+def test_scalar_restatement_vs_reference_scalar():
+    b = synth.generate(synth.C2.scaled(2000, seed=77))
+    P = synth.C2.params()
+    r = oracle.reference(b.pairs, b.ref, b.qer, 100, P, mode=0)
+    s, cells = oracle.scalar(b.pairs, b.ref, b.qer, 100, P)
+    assert (outputs(r) == outputs(s)).all()
+    assert cells > 0
+
+
+def test_scalar_equals_vector_at_unit_gap_extension():
+    """At e_del = e_ins = 1 the reference's vector z-drop (which drops the
+    gap-extension weight) coincides with the scalar one, so scalarBandedSWA and
+    getScores16 agree -- the basis of the scalar CPU baseline."""
+    b = synth.generate(synth.C1.scaled(1500, seed=5))
+    P = synth.C1.params()
+    s, _ = oracle.scalar(b.pairs, b.ref, b.qer, 100, P)
+    v = oracle.vector(b.pairs, b.ref, b.qer, 100, P, bits=16)
+    assert (outputs(s) == outputs(v)).all()
+
+
+def test_eligible8_rule():
+    b = synth.generate(synth.C1_8, 500)
+    assert oracle.eligible8(b.pairs, 100, synth.C1_8.params()).all()
+    c = synth.generate(synth.C1, 50)
+    assert not oracle.eligible8(c.pairs, 100, synth.C1.params()).any()
+
+
+def test_planted_mistake_is_caught():
+    """A checker that cannot fail is no checker: perturb one oracle output and
+    the comparison must notice."""
+    d, P = _load(FILES[0])
+    got = oracle.routed(d["inputs"], d["ref"], d["qer"], d["w"], P, bits=int(d["bits"]))
+    got["score"][3] += 1
+    assert not (outputs(got) == outputs(d["expected"])).all()

@@ -1,0 +1,364 @@
+// C ABI of the GB300 banded Smith-Waterman (include/tal_bsw.h): handle
+// management, host<->device staging and kernel launches.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <climits>
+#include <mutex>
+#include <string>
+
+#include "../../include/tal_bsw.h"
+#include "bsw_kernel.cuh"
+
+static_assert(sizeof(tal_seq_pair) == 56, "SeqPair is 14 x int32 (bandedSWA.h:90-99)");
+static_assert(sizeof(talbsw::DevPair) == 56, "device SeqPair view");
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max(bytes, cap + cap / 2);
+        want = (want + 255) & ~(size_t)255;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct tal_bsw_ctx {
+    tal_bsw_params prm;
+    talbsw::KernelParams kp;
+    int device = 0;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf pairs, ref, qer, ctrl, wpair, caps;
+    std::mutex mu;
+    std::string last_error;
+    int64_t last_bad = -1;
+    uint64_t launches = 0;
+    int pending_status = TAL_OK;
+    int forced_K = 0;
+};
+
+namespace {
+
+int fail(tal_bsw_ctx *h, int code, const std::string &msg) {
+    if (h) h->last_error = msg;
+    return code;
+}
+
+int cuda_fail(tal_bsw_ctx *h, cudaError_t e, const char *what) {
+    return fail(h, TAL_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// control block on the device: work counter, error flags, first bad index
+struct Ctrl {
+    int counter;
+    int flags;
+    long long bad_index;
+};
+
+template <int K>
+cudaError_t launch_k(tal_bsw_ctx *h, const talbsw::LaunchArgs &A, int wpb, size_t smem) {
+    auto kern = talbsw::bsw_warp_kernel<K>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    int bps = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, smem);
+    if (e != cudaSuccess) return e;
+    if (bps < 1) return cudaErrorInvalidConfiguration;
+    long long blocks = (long long)bps * h->num_sms;
+    long long need = ((long long)A.n + wpb - 1) / wpb;
+    if (blocks > need) blocks = std::max<long long>(need, 1);
+    kern<<<(unsigned)blocks, 32 * wpb, smem, h->stream>>>(A);
+    h->launches++;
+    return cudaGetLastError();
+}
+
+int pick_k(tal_bsw_ctx *h, int w, int cols_cap) {
+    if (h->forced_K == 1 || h->forced_K == 2 || h->forced_K == 4) return h->forced_K;
+    long long band = std::min<long long>(2LL * std::max(w, 0) + 1, (long long)cols_cap);
+    if (band <= 40) return 1;
+    if (band <= 100) return 2;
+    return 4;
+}
+
+// Issues the scoring launch for pairs already on the device.
+int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
+    Ctrl *c = reinterpret_cast<Ctrl *>(h->ctrl.p);
+    A.work_counter = &c->counter;
+    A.err_flags = &c->flags;
+    A.err_index = &c->bad_index;
+    A.P = h->kp;
+    const int K = pick_k(h, w_for_k, A.cols_cap);
+    size_t wbytes = talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, K);
+    int wpb = 4;
+    while (wpb > 1 && (size_t)wpb * wbytes * 2 > h->smem_optin) wpb >>= 1;
+    size_t smem = (size_t)wpb * wbytes;
+    if (smem > h->smem_optin)
+        return fail(h, TAL_EDOMAIN, "pair too long for the shared-memory row buffers");
+    Ctrl init = {0, 0, (long long)INT64_MAX};
+    cudaError_t e = cudaMemcpyAsync(c, &init, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(ctrl)");
+    if (K == 1) e = launch_k<1>(h, A, wpb, smem);
+    else if (K == 2) e = launch_k<2>(h, A, wpb, smem);
+    else e = launch_k<4>(h, A, wpb, smem);
+    if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
+    return TAL_OK;
+}
+
+int collect(tal_bsw_ctx *h) {
+    Ctrl c;
+    cudaError_t e = cudaMemcpyAsync(&c, h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "scoring");
+    if (c.flags) {
+        h->last_bad = c.bad_index;
+        std::string why;
+        if (c.flags & talbsw::ERR_DOMAIN) why += "pair outside the exact 8/16-bit range; ";
+        if (c.flags & talbsw::ERR_CAPACITY) why += "pair longer than the row capacity; ";
+        if (c.flags & talbsw::ERR_BASE) why += "base code above 4; ";
+        return fail(h, TAL_EDOMAIN, why + "first bad pair " + std::to_string(c.bad_index));
+    }
+    return TAL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tal_bsw_create(const tal_bsw_params *params, int device, tal_bsw_handle *out) {
+    if (!params || !out) return TAL_EINVAL;
+    *out = nullptr;
+    const tal_bsw_params &p = *params;
+    auto in = [](int v, int lo, int hi) { return v >= lo && v <= hi; };
+    if (!in(p.o_del, 0, 127) || !in(p.o_ins, 0, 127) || !in(p.e_del, 1, 127) ||
+        !in(p.e_ins, 1, 127) || !in(p.w_match, 0, 127) || !in(p.w_mismatch, 0, 127))
+        return TAL_EINVAL;
+    int dev = device;
+    cudaError_t e;
+    if (dev < 0) {
+        e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return TAL_ENODEV;
+    }
+    e = cudaSetDevice(dev);
+    if (e != cudaSuccess) return TAL_ENODEV;
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return TAL_ENODEV;
+    if (prop.major != 10) return TAL_ENODEV;
+    tal_bsw_ctx *h = new (std::nothrow) tal_bsw_ctx();
+    if (!h) return TAL_ENOMEM;
+    h->prm = p;
+    h->kp = {p.o_del, p.e_del, p.o_ins, p.e_ins, p.zdrop, p.end_bonus, p.w_match, p.w_mismatch};
+    h->device = dev;
+    h->num_sms = prop.multiProcessorCount;
+    h->smem_optin = prop.sharedMemPerBlockOptin;
+    if (const char *k = getenv("TAL_BSW_K")) h->forced_K = atoi(k);
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = h->ctrl.ensure(sizeof(Ctrl));
+    if (e != cudaSuccess) {
+        if (h->stream) cudaStreamDestroy(h->stream);
+        h->ctrl.release();
+        delete h;
+        return e == cudaErrorMemoryAllocation ? TAL_ENOMEM : TAL_ECUDA;
+    }
+    *out = h;
+    return TAL_OK;
+}
+
+int tal_bsw_destroy(tal_bsw_handle h) {
+    if (!h) return TAL_EINVAL;
+    {
+        std::lock_guard<std::mutex> lk(h->mu);
+        cudaSetDevice(h->device);
+        cudaStreamSynchronize(h->stream);
+        h->pairs.release();
+        h->ref.release();
+        h->qer.release();
+        h->ctrl.release();
+        h->wpair.release();
+        h->caps.release();
+        cudaStreamDestroy(h->stream);
+    }
+    delete h;
+    return TAL_OK;
+}
+
+int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufRef,
+                   const uint8_t *seqBufQer, int32_t numPairs, int32_t w, int bits) {
+    if (!h) return TAL_EINVAL;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->last_error.clear();
+    h->last_bad = -1;
+    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16))
+        return fail(h, TAL_EINVAL, "bad numPairs or bits");
+    if (numPairs == 0) return TAL_OK;
+    if (!pairs || !seqBufRef || !seqBufQer) return fail(h, TAL_EINVAL, "NULL buffer");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    // extents of the byte windows the pairs reference, and row capacities
+    long long rlo = LLONG_MAX, rhi = 0, qlo = LLONG_MAX, qhi = 0;
+    int max1 = 0, max2 = 0;
+    for (int32_t k = 0; k < numPairs; k++) {
+        const tal_seq_pair &p = pairs[k];
+        if (p.len1 < 0 || p.len2 < 0 || p.idr < 0 || p.idq < 0) {
+            h->last_bad = k;
+            return fail(h, TAL_EDOMAIN, "negative length or offset at pair " + std::to_string(k));
+        }
+        rlo = std::min<long long>(rlo, p.idr);
+        qlo = std::min<long long>(qlo, p.idq);
+        rhi = std::max<long long>(rhi, (long long)p.idr + p.len1);
+        qhi = std::max<long long>(qhi, (long long)p.idq + p.len2);
+        max1 = std::max(max1, p.len1);
+        max2 = std::max(max2, p.len2);
+    }
+    rlo &= ~15LL;
+    qlo &= ~15LL;
+    if (rhi <= rlo) rhi = rlo + 16;
+    if (qhi <= qlo) qhi = qlo + 16;
+    const size_t pbytes = (size_t)numPairs * sizeof(tal_seq_pair);
+    if ((e = h->pairs.ensure(pbytes)) != cudaSuccess ||
+        (e = h->ref.ensure((size_t)(rhi - rlo) + 16)) != cudaSuccess ||
+        (e = h->qer.ensure((size_t)(qhi - qlo) + 16)) != cudaSuccess)
+        return fail(h, TAL_ENOMEM, std::string("device buffers: ") + cudaGetErrorString(e));
+    e = cudaMemcpyAsync(h->pairs.p, pairs, pbytes, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->ref.p, seqBufRef + rlo, (size_t)(rhi - rlo),
+                            cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->qer.p, seqBufQer + qlo, (size_t)(qhi - qlo),
+                            cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(H2D)");
+    talbsw::LaunchArgs A;
+    memset(&A, 0, sizeof(A));
+    A.pairs = reinterpret_cast<talbsw::DevPair *>(h->pairs.p);
+    A.ref = reinterpret_cast<const uint8_t *>(h->ref.p);
+    A.qer = reinterpret_cast<const uint8_t *>(h->qer.p);
+    A.ref_lo = rlo; A.ref_hi = rhi; A.qer_lo = qlo; A.qer_hi = qhi;
+    A.order = nullptr;
+    A.wpair = nullptr;
+    A.n = numPairs;
+    A.w = w;
+    A.bits = bits;
+    A.cols_cap = std::max(max2, 1);
+    A.rows_cap = std::max(max1, 1);
+    int rc = launch_scoring(h, A, w);
+    if (rc != TAL_OK) {
+        cudaStreamSynchronize(h->stream);
+        return rc;
+    }
+    rc = collect(h);
+    if (rc != TAL_OK) return rc;
+    e = cudaMemcpyAsync(pairs, h->pairs.p, pbytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(D2H)");
+    return TAL_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// max len1 / len2 over a device SeqPair array (or a per-pair band), for
+// sizing the shared-memory rows of a device-resident call
+__global__ void caps_kernel(const talbsw::DevPair *p, int n, int *out) {
+    int m1 = 0, m2 = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        m1 = max(m1, p[k].len1);
+        m2 = max(m2, p[k].len2);
+    }
+    m1 = __reduce_max_sync(0xffffffffu, (unsigned)max(m1, 0));
+    m2 = __reduce_max_sync(0xffffffffu, (unsigned)max(m2, 0));
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out + 0, m1);
+        atomicMax(out + 1, m2);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int tal_bsw_scores_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t *d_ref,
+                          size_t ref_bytes, const uint8_t *d_qer, size_t qer_bytes,
+                          int32_t numPairs, int32_t w, const int32_t *d_w, int bits) {
+    if (!h) return TAL_EINVAL;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->last_error.clear();
+    h->last_bad = -1;
+    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16))
+        return fail(h, TAL_EINVAL, "bad numPairs or bits");
+    if (numPairs == 0) return TAL_OK;
+    if (!d_pairs || !d_ref || !d_qer) return fail(h, TAL_EINVAL, "NULL buffer");
+    if (((uintptr_t)d_ref & 15) || ((uintptr_t)d_qer & 15))
+        return fail(h, TAL_EINVAL, "device sequence buffers must be 16-byte aligned");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    if ((e = h->caps.ensure(2 * sizeof(int))) != cudaSuccess)
+        return fail(h, TAL_ENOMEM, "caps buffer");
+    int *caps = reinterpret_cast<int *>(h->caps.p);
+    e = cudaMemsetAsync(caps, 0, 2 * sizeof(int), h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
+    int blocks = std::min<long long>(((long long)numPairs + 255) / 256, (long long)h->num_sms * 8);
+    caps_kernel<<<blocks, 256, 0, h->stream>>>(reinterpret_cast<talbsw::DevPair *>(d_pairs),
+                                                numPairs, caps);
+    h->launches++;
+    int hc[2] = {0, 0};
+    e = cudaMemcpyAsync(hc, caps, sizeof(hc), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "caps");
+    talbsw::LaunchArgs A;
+    memset(&A, 0, sizeof(A));
+    A.pairs = reinterpret_cast<talbsw::DevPair *>(d_pairs);
+    A.ref = d_ref;
+    A.qer = d_qer;
+    A.ref_lo = 0; A.ref_hi = (long long)ref_bytes;
+    A.qer_lo = 0; A.qer_hi = (long long)qer_bytes;
+    A.wpair = d_w;
+    A.n = numPairs;
+    A.w = w;
+    A.bits = bits;
+    A.cols_cap = std::max(hc[1], 1);
+    A.rows_cap = std::max(hc[0], 1);
+    int rc = launch_scoring(h, A, w);
+    if (rc != TAL_OK) return rc;
+    h->pending_status = TAL_OK;
+    return TAL_OK;
+}
+
+int tal_bsw_sync(tal_bsw_handle h) {
+    if (!h) return TAL_EINVAL;
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    return collect(h);
+}
+
+void *tal_bsw_stream(tal_bsw_handle h) { return h ? (void *)h->stream : nullptr; }
+
+const char *tal_bsw_last_error(tal_bsw_handle h) { return h ? h->last_error.c_str() : "null handle"; }
+
+int64_t tal_bsw_last_bad_pair(tal_bsw_handle h) { return h ? h->last_bad : -1; }
+
+uint64_t tal_bsw_launch_count(tal_bsw_handle h) { return h ? h->launches : 0; }
+
+}  // extern "C"

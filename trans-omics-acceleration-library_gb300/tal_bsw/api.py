@@ -1,0 +1,172 @@
+"""Python mirror of the reference's BandedPairWiseSW (src/alignment/BSW/bandedSWA.h:113-336)
+over the C ABI in include/tal_bsw.h.
+
+    bsw = BandedPairWiseSW(o_del, e_del, o_ins, e_ins, zdrop, end_bonus, mat, w_match,
+                           w_mismatch, numThreads)
+    bsw.getScores16(pairArray, seqBufRef, seqBufQer, numPairs, numThreads, w)
+
+Same names, argument order and meaning as the reference; ``pairArray`` is a numpy
+array of SeqPair records (tal_bsw.seqpair.SEQPAIR_DTYPE) updated in place.  Where
+the reference exits the process on failure (bandedSWA.cpp:88-93), this raises
+TalBswError.  There is no CPU fallback: without the CUDA library or a GB300 the
+constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from ._lib import load_core
+from .seqpair import SEQPAIR_DTYPE
+
+TAL_OK, TAL_EINVAL, TAL_EDOMAIN, TAL_ENOMEM, TAL_ECUDA, TAL_ETIMEOUT, TAL_ENODEV, TAL_EBUSY = range(8)
+STATUS_NAMES = {0: "TAL_OK", 1: "TAL_EINVAL", 2: "TAL_EDOMAIN", 3: "TAL_ENOMEM", 4: "TAL_ECUDA",
+                5: "TAL_ETIMEOUT", 6: "TAL_ENODEV", 7: "TAL_EBUSY"}
+AUTO, BITS8, BITS16 = 0, 8, 16
+
+
+class TalBswError(RuntimeError):
+    def __init__(self, status: int, message: str, bad_pair: int = -1):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+        self.bad_pair = bad_pair
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in
+                ("o_del", "e_del", "o_ins", "e_ins", "zdrop", "end_bonus", "w_match", "w_mismatch")]
+
+
+_SIGS = {
+    "tal_bsw_create": (ctypes.c_int, [ctypes.POINTER(_Params), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "tal_bsw_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tal_bsw_scores": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_int]),
+    "tal_bsw_scores_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                             ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.c_void_p, ctypes.c_int]),
+    "tal_bsw_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "tal_bsw_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "tal_bsw_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "tal_bsw_last_bad_pair": (ctypes.c_int64, [ctypes.c_void_p]),
+    "tal_bsw_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
+}
+
+
+def core_lib():
+    lib = load_core()
+    if not getattr(lib, "_tal_typed", False):
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        lib._tal_typed = True
+    return lib
+
+
+def _as_pairs(pairArray: np.ndarray) -> np.ndarray:
+    if not isinstance(pairArray, np.ndarray) or pairArray.dtype != SEQPAIR_DTYPE:
+        raise TypeError("pairArray must be a numpy array of SEQPAIR_DTYPE records")
+    if not pairArray.flags["C_CONTIGUOUS"] or not pairArray.flags["WRITEABLE"]:
+        raise TypeError("pairArray must be C-contiguous and writeable (updated in place)")
+    return pairArray
+
+
+def _buf_ptr(buf) -> int:
+    if isinstance(buf, np.ndarray):
+        if buf.dtype != np.uint8 or not buf.flags["C_CONTIGUOUS"]:
+            raise TypeError("sequence buffers must be contiguous uint8 arrays")
+        return buf.ctypes.data
+    if isinstance(buf, int):
+        return buf
+    raise TypeError("sequence buffer must be a uint8 numpy array or an address")
+
+
+class BandedPairWiseSW:
+    """GB300 drop-in for the reference class.  ``mat`` is accepted and ignored,
+    as by the reference's vector kernels (bandedSWA.cpp:1883-1892)."""
+
+    def __init__(self, o_del: int, e_del: int, o_ins: int, e_ins: int, zdrop: int,
+                 end_bonus: int, mat=None, w_match: int = 1, w_mismatch: int = 4,
+                 numThreads: int = 1, device: int = -1):
+        self._lib = core_lib()
+        self.params = dict(o_del=o_del, e_del=e_del, o_ins=o_ins, e_ins=e_ins, zdrop=zdrop,
+                           end_bonus=end_bonus, a=w_match, b=w_mismatch)
+        p = _Params(o_del, e_del, o_ins, e_ins, zdrop, end_bonus, w_match, w_mismatch)
+        h = ctypes.c_void_p()
+        rc = self._lib.tal_bsw_create(ctypes.byref(p), int(device), ctypes.byref(h))
+        if rc != TAL_OK:
+            raise TalBswError(rc, "tal_bsw_create failed (parameters out of range or no GB300)")
+        self._h = h
+        self.SW_cells = 0
+
+    # -- reference entry points -------------------------------------------------
+    def getScores8(self, pairArray, seqBufRef, seqBufQer, numPairs: int, numThreads: int = 1,
+                   w: int = 100) -> None:
+        self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, BITS8)
+
+    def getScores16(self, pairArray, seqBufRef, seqBufQer, numPairs: int, numThreads: int = 1,
+                    w: int = 100) -> None:
+        self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, BITS16)
+
+    def getScoresAuto(self, pairArray, seqBufRef, seqBufQer, numPairs: int,
+                      numThreads: int = 1, w: int = 100) -> None:
+        """Each pair to the 8-bit kernel when it is inside the 8-bit range,
+        else to the 16-bit kernel."""
+        self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, AUTO)
+
+    # -- device-resident form -------------------------------------------------------
+    def scores_device(self, d_pairs: int, d_ref: int, ref_bytes: int, d_qer: int, qer_bytes: int,
+                      numPairs: int, w: int, bits: int = BITS16, d_w: Optional[int] = None,
+                      sync: bool = True) -> None:
+        rc = self._lib.tal_bsw_scores_device(self._h, d_pairs, d_ref, ref_bytes, d_qer, qer_bytes,
+                                             int(numPairs), int(w), d_w, int(bits))
+        self._check(rc)
+        if sync:
+            self.sync()
+
+    def sync(self) -> None:
+        self._check(self._lib.tal_bsw_sync(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.tal_bsw_stream(self._h) or 0)
+
+    @property
+    def launch_count(self) -> int:
+        return int(self._lib.tal_bsw_launch_count(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.tal_bsw_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- internals ------------------------------------------------------------------
+    def _check(self, rc: int) -> None:
+        if rc != TAL_OK:
+            msg = self._lib.tal_bsw_last_error(self._h)
+            bad = int(self._lib.tal_bsw_last_bad_pair(self._h))
+            raise TalBswError(rc, (msg or b"").decode(), bad)
+
+    def _scores(self, pairArray, seqBufRef, seqBufQer, numPairs, w, bits) -> None:
+        pa = _as_pairs(pairArray)
+        n = int(numPairs)
+        if n < 0 or n > pa.shape[0]:
+            raise ValueError("numPairs out of range for pairArray")
+        rc = self._lib.tal_bsw_scores(self._h, pa.ctypes.data, _buf_ptr(seqBufRef),
+                                      _buf_ptr(seqBufQer), n, int(w), int(bits))
+        self._check(rc)
