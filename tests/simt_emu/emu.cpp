@@ -1,0 +1,86 @@
+// Runs the CUDA kernel source (csrc/bsw_kernel.cuh), compiled for the host,
+// one std::thread per lane, so its logic can be checked against the oracle on
+// a machine without a GPU.  Test infrastructure only; the product path never
+// uses it.
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "cuda_runtime.h"
+
+namespace simt {
+thread_local Dim tl_threadIdx, tl_blockIdx, tl_blockDim, tl_gridDim;
+thread_local Warp *tl_warp;
+thread_local unsigned char *tl_smem;
+std::mutex atomic_mu;
+}  // namespace simt
+
+// The kernel's dynamic shared memory resolves to the per-block buffer.
+#define TALBSW_DYNAMIC_SMEM(name) unsigned char *name = simt::tl_smem
+#include "bsw_kernel.cuh"
+
+extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long ref_lo,
+                           long long ref_hi, const uint8_t *qer, long long qer_lo,
+                           long long qer_hi, int n, int w, const int32_t *wpair, int bits,
+                           const int32_t *kp, int K, int warps, int *err_flags,
+                           long long *err_index) {
+    talbsw::LaunchArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.pairs = pairs;
+    A.ref = ref; A.ref_lo = ref_lo; A.ref_hi = ref_hi;
+    A.qer = qer; A.qer_lo = qer_lo; A.qer_hi = qer_hi;
+    A.wpair = wpair;
+    A.n = n; A.w = w; A.bits = bits;
+    int m1 = 1, m2 = 1;
+    for (int i = 0; i < n; i++) { m1 = std::max(m1, pairs[i].len1); m2 = std::max(m2, pairs[i].len2); }
+    A.cols_cap = m2; A.rows_cap = m1;
+    int counter = 0;
+    *err_flags = 0; *err_index = (long long)INT64_MAX;
+    A.work_counter = &counter; A.err_flags = err_flags; A.err_index = err_index;
+    A.P = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], kp[6], kp[7]};
+    size_t wbytes = talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, K);
+    std::vector<unsigned char> smem(wbytes * warps + 64, 0xA5);  // poisoned, like fresh smem
+    // warps run one after another; the 32 lanes of a warp are fibers
+    int divergent = 0;
+    for (int wi = 0; wi < warps; wi++) {
+        simt::Warp *W = new simt::Warp();
+        std::vector<std::vector<char>> stacks(32, std::vector<char>(1 << 18));
+        struct Arg { int t; simt::Warp *W; const talbsw::LaunchArgs *A; int K; unsigned char *sm; int warps; };
+        static thread_local Arg args[32];
+        for (int l = 0; l < 32; l++) {
+            args[l] = Arg{wi * 32 + l, W, &A, K, smem.data(), warps};
+            getcontext(&W->lane_ctx[l]);
+            W->lane_ctx[l].uc_stack.ss_sp = stacks[l].data();
+            W->lane_ctx[l].uc_stack.ss_size = stacks[l].size();
+            W->lane_ctx[l].uc_link = &W->sched;
+            makecontext(&W->lane_ctx[l], (void (*)())+[](int l2) {
+                Arg &a = args[l2];
+                simt::tl_threadIdx.x = a.t;
+                simt::tl_blockIdx.x = 0;
+                simt::tl_blockDim.x = 32 * a.warps;
+                simt::tl_gridDim.x = 1;
+                simt::tl_warp = a.W;
+                simt::tl_smem = a.sm;
+                if (a.K == 1) talbsw::bsw_warp_kernel<1>(*a.A);
+                else if (a.K == 2) talbsw::bsw_warp_kernel<2>(*a.A);
+                else talbsw::bsw_warp_kernel<4>(*a.A);
+                a.W->done[a.t & 31] = true;
+            }, 1, l);
+        }
+        for (;;) {
+            int ndone = 0;
+            for (int l = 0; l < 32; l++) {
+                if (W->done[l]) { ndone++; continue; }
+                simt::tl_warp = W;
+                simt::tl_threadIdx.x = wi * 32 + l;
+                swapcontext(&W->sched, &W->lane_ctx[l]);
+                if (W->done[l]) ndone++;
+            }
+            if (ndone == 32) break;
+            if (ndone > 0) { divergent = 1; break; }
+        }
+        delete W;
+    }
+    if (divergent) return -1;
+    return 0;
+}

@@ -30,6 +30,12 @@
 #include <stdint.h>
 #include <cuda_runtime.h>
 
+// The per-block dynamic shared memory; a host build of this file for the
+// CPU emulator in the tests defines the macro to a plain pointer first.
+#ifndef TALBSW_DYNAMIC_SMEM
+#define TALBSW_DYNAMIC_SMEM(name) extern __shared__ __align__(16) unsigned char name[]
+#endif
+
 namespace talbsw {
 
 struct KernelParams {
@@ -201,7 +207,7 @@ __device__ __forceinline__ bool stage_bases(uint8_t *dst, const uint8_t *src, in
 
 template <int K>
 __global__ void __launch_bounds__(128) bsw_warp_kernel(LaunchArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TALBSW_DYNAMIC_SMEM(smem_raw);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const size_t wbytes = warp_smem_bytes(A.cols_cap, A.rows_cap, K);
@@ -344,20 +350,21 @@ __global__ void __launch_bounds__(128) bsw_warp_kernel(LaunchArgs A) {
             // row exit status (:3119-3129); outputs freeze once a pair exits
             if (i1 > mlen || tail == head || head > tail) break;
 
-            // score lookup for this row's target base: bytes 0..3 = query
-            // base 0..3, byte 4 (thi) = query N; sign-extended by PRMT
+            // score lookup for this row's target base: byte q of {thi:tlo} is
+            // S(t, q) + 128 for query code q (0..3 bases, 4 = N); bytes 5..7 are
+            // zero so a selector q | 0x7770 yields the byte zero-extended
             const int tb = Tt[i];
             uint32_t tlo, thi;
             {
-                const uint32_t bb = (uint32_t)(uint8_t)(int8_t)(-P.b);
-                const uint32_t ab = (uint32_t)(uint8_t)(int8_t)P.a;
+                const uint32_t mis = (uint32_t)(128 - P.b) & 0xffu;
+                const uint32_t mat = (uint32_t)(128 + P.a) & 0xffu;
                 if (tb >= 4) {
-                    tlo = 0xffffffffu;
+                    tlo = 0x7f7f7f7fu;  // N in the target: -1 against anything
                 } else {
-                    tlo = bb * 0x01010101u;
-                    tlo = (tlo & ~(0xffu << (8 * tb))) | (ab << (8 * tb));
+                    tlo = mis * 0x01010101u;
+                    tlo = (tlo & ~(0xffu << (8 * tb))) | (mat << (8 * tb));
                 }
-                thi = 0x000000ffu;
+                thi = 0x0000007fu;      // N in the query: -1
             }
 
             // ---- the row, strip by strip
@@ -387,8 +394,8 @@ __global__ void __launch_bounds__(128) bsw_warp_kernel(LaunchArgs A) {
                     const int h00 = (int)(hf[k] & 0xffffu);
                     const int f11 = (int)(hf[k] >> 16);
                     const uint32_t q = (qv >> (8 * k)) & 0xffu;
-                    const int sbt = (int)__byte_perm(tlo, thi, q * 0x1111u + 0x8880u);
-                    const int m = h00 ? h00 + sbt : 0;
+                    const int sbt = (int)__byte_perm(tlo, thi, q | 0x7770u);  // S + 128
+                    const int m = h00 ? h00 + sbt - 128 : 0;
                     mm[k] = m;
                     ff[k] = f11;
                     const int Pk = imax(m - oe_insE, 0) + e_insE * (j - beg);
