@@ -1,0 +1,427 @@
+#!/usr/bin/env python
+"""Benchmark of the banded Smith-Waterman seed extension on GB300.
+
+Metric: BSW GCUPS (reference cells per second; a cell is one iteration of the
+reference's scalar inner loop, bandedSWA.cpp:175-200) and pairs/s.  A step is
+one pass of the hot path over one batch: at N=1 the 16-bit plain-launch
+workload, 1,000,000 seeded synthetic pairs (query U[100,300] bp, 4% subs +
+0.5% 1-5 bp indels, len1 = len2 + U[0,40], h0 ~ U[30,250], w = 100,
+zdrop = 100), scored with getScores16 semantics.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is measured with the inputs resident in HBM (device-resident call,
+CUDA events on the library's stream); `e2e` goes through the reference-facing
+C ABI call (tal_bsw_scores) with pinned host buffers, host<->device copies
+inside the timed region.  Under torchrun each rank scores its own shard of
+pairs (independent pairs, no collective): weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "trans-omics-acceleration-library_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "BSW GCUPS & pairs/s, batched vs plain launch on 1 GB300 (bit-exact); p99 latency"
+UNIT = "GCUPS"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="c2_16bit")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="CPU work for the cpu_baseline sample (rank 0, N=1)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling)")
+    ap.add_argument("--pairs", type=int, default=None,
+                    help="score only the first N pairs of the workload (profiling a small case)")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------- helpers
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, backend):
+        self.ws, self.rank, self.local = dist_info()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group(backend=backend)
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        dev = f"cuda:{self.local}" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        dev = f"cuda:{self.local}" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows
+                                    if r[3].replace(".", "").isdigit()), default=None)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def workload_cells(name):
+    p = os.path.join(PKG, "tal_bsw", "workload_cells.json")
+    d = json.load(open(p)) if os.path.exists(p) else {}
+    return d.get(name)
+
+
+def profile_traffic(name):
+    """dram bytes per launch of the main kernel from the committed ncu
+    summary, if one covers this workload."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    e = d.get(name)
+    return None if e is None else e.get("dram_bytes_per_launch")
+
+
+# ---------------------------------------------------------------------- CPU baseline
+def cpu_score(batch, wl, nthreads):
+    """Times the CPU implementation on `batch`; returns (seconds, ref-cells,
+    kind, description).  The reference itself where it was compiled on this
+    host (x86 with AVX-512: getScores16 from oracle/_ref, one instance per
+    thread), else the oracle's port of scalarBandedSWAWrapper (the
+    reference's portable path, equal to getScores16 at e_del = e_ins = 1)."""
+    import oracle
+    P = wl.params()
+    bits = 8 if wl.bits == 8 else 16
+    if oracle.ref_available("avx512"):
+        parts = np.array_split(np.arange(batch.n), nthreads)
+        t = time.perf_counter()
+        with cf.ThreadPoolExecutor(nthreads) as ex:
+            list(ex.map(lambda ix: oracle.reference(batch.pairs[ix], batch.ref, batch.qer,
+                                                    wl.w, P, mode=bits, pristine=False), parts))
+        dt = time.perf_counter() - t
+        _, cells = oracle.scalar(batch.pairs, batch.ref, batch.qer, wl.w, P, nthreads=nthreads)
+        return dt, cells, "reference", f"getScores{bits} (AVX-512BW build of the reference)"
+    t = time.perf_counter()
+    _, cells = oracle.scalar(batch.pairs, batch.ref, batch.qer, wl.w, P, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    return dt, cells, "port", "oracle port of scalarBandedSWAWrapper (bandedSWA.cpp:116-260)"
+
+
+def cpu_sample(wl, seconds, nthreads, first=0):
+    """A batch of the workload sized for about `seconds` of CPU work."""
+    from tal_bsw import synth
+    n = 2000
+    probe = synth.generate(wl, n, first=first)
+    dt, cells, _, _ = cpu_score(probe, wl, nthreads)
+    rate = n / max(dt, 1e-3)
+    n2 = int(min(wl.n_pairs, max(n, rate * seconds)))
+    return synth.generate(wl, n2, first=first)
+
+
+def cpu_isa():
+    import platform
+    m = platform.machine()
+    model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    return f"{m} {model}".strip()
+
+
+# -------------------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+    import tal_bsw
+    from tal_bsw import synth
+    from tal_bsw.api import probe_int_peak
+
+    dist = Dist("nccl")
+    ws, rank, local = dist.ws, dist.rank, dist.local
+    torch.cuda.set_device(local)
+    wl = synth.WORKLOADS[args.workload]
+    n = wl.n_pairs if not args.pairs else min(args.pairs, wl.n_pairs)
+    first = rank * n                       # each rank its own shard of pairs
+    b = synth.generate(wl, n, first=first)
+    P = wl.params()
+    bits = 8 if wl.bits == 8 else 16
+    cinfo = workload_cells(wl.name)
+
+    bsw = tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                   P["end_bonus"], None, P["a"], P["b"], 1, device=local)
+    stream = torch.cuda.ExternalStream(bsw.stream)
+    pairs_u8 = b.pairs.view(np.uint8).reshape(-1)
+    dp = torch.from_numpy(pairs_u8.copy()).cuda()
+    dr = torch.from_numpy(b.ref).cuda()
+    dq = torch.from_numpy(b.qer).cuda()
+    torch.cuda.synchronize()
+
+    def step_device():
+        bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                          n, wl.w, bits)
+
+    for _ in range(max(args.warmup, 3)):
+        step_device()
+    kernel_cells = bsw.last_cells
+    # ref-cells of this shard: counted once per workload (rank 0's shard is
+    # the workload itself); other shards scale the kernel's own count
+    counted = bool(cinfo) and rank == 0 and cinfo["n_pairs"] == n
+    ratio = dist.max(int(cinfo["ref_cells"]) / max(kernel_cells, 1) if counted else 0.0)
+    ref_cells = int(cinfo["ref_cells"]) if counted else int(kernel_cells * (ratio or 1.0))
+
+    # ---- device-resident timed region
+    clocks = ClockSampler(local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = bsw.launch_count
+    clocks.start()
+    time.sleep(0.3)
+    e0.record(stream)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_device()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = bsw.launch_count - launches0
+    dist.barrier()
+    t_step = e0.elapsed_time(e1) / 1e3 / args.steps
+    t_step_max = dist.max(t_step)
+    total_cells = dist.sum(float(ref_cells))
+    total_pairs = n * ws
+    value = total_cells / t_step_max / 1e9
+
+    # ---- end to end through the C ABI, host buffers pinned
+    if args.no_e2e:
+        print(json.dumps({"value": value, "unit": UNIT, "ms_per_step": t_step_max * 1e3,
+                          "pairs": n, "gpu_launches": launches}), flush=True)
+        bsw.close()
+        dist.close()
+        return
+    hp = torch.empty(pairs_u8.shape[0], dtype=torch.uint8, pin_memory=True)
+    hr = torch.empty(b.ref.shape[0], dtype=torch.uint8, pin_memory=True)
+    hq = torch.empty(b.qer.shape[0], dtype=torch.uint8, pin_memory=True)
+    hp.numpy()[:] = pairs_u8
+    hr.numpy()[:] = b.ref
+    hq.numpy()[:] = b.qer
+    hpairs = hp.numpy().view(tal_bsw.SEQPAIR_DTYPE)
+    e2e_steps = args.e2e_steps or max(3, args.steps // 2)
+    for _ in range(2):
+        bsw.getScores16(hpairs, hr.numpy(), hq.numpy(), n, 1, wl.w) if bits == 16 else \
+            bsw.getScores8(hpairs, hr.numpy(), hq.numpy(), n, 1, wl.w)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        if bits == 16:
+            bsw.getScores16(hpairs, hr.numpy(), hq.numpy(), n, 1, wl.w)
+        else:
+            bsw.getScores8(hpairs, hr.numpy(), hq.numpy(), n, 1, wl.w)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    t_e2e_max = dist.max(t_e2e)
+    e2e_value = total_cells / t_e2e_max / 1e9
+    lens = int(b.pairs["len1"].sum() + b.pairs["len2"].sum())
+    h2d = pairs_u8.nbytes + int(b.pairs["len1"].sum()) + int(b.pairs["len2"].sum())
+    d2h = pairs_u8.nbytes
+    # parity guard on the timed outputs: device-resident and host paths agree
+    dev_out = dp.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE)
+    agree = bool((tal_bsw.outputs(dev_out) == tal_bsw.outputs(hpairs)).all())
+
+    # ---- rooflines
+    hbm_peak, peak_src = measured_peaks()
+    alg_bytes = lens + 56 * n + 24 * n          # bases read, SeqPair read, outputs written
+    achieved = alg_bytes / t_step / 1e9
+    dpx, i32 = probe_int_peak(local)
+    int_cells_peak = dpx / 4.0                   # 8 int16 lane-ops per cell, 2 lanes per DPX op
+
+    result = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": round(t_step_max * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int16", "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": f"{wl.name}: {n} pairs, query U[{wl.len_lo},{wl.len_hi}], "
+                               f"w={wl.w}, zdrop={wl.zdrop}, getScores{bits} plain launch",
+                   "pairs_per_step": total_pairs, "ref_cells_per_step": int(total_cells),
+                   "kernel_cells_per_step": int(kernel_cells) * ws,
+                   "l2": "inputs larger than L2 (no flush needed)",
+                   "parallelism": f"replica shards x{ws}, no collective"},
+        "pairs_per_s": round(total_pairs / t_step_max, 1),
+        "wall_s_timed": round(wall, 3),
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "pairs_per_s": round(total_pairs / t_e2e_max, 1),
+                "ms_per_step": round(t_e2e_max * 1e3, 3), "outputs_match_device_path": agree},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm_peak,
+                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
+                     "traffic": profile_traffic(wl.name), "peak_source": peak_src,
+                     "note": "integer-pipe bound kernel; see roofline_int"},
+        "roofline_int": {"bound": "int (DPX 16x2)", "achieved": round(value * 1e9 / ws, 1),
+                         "peak": round(int_cells_peak, 1), "unit": "cells/s",
+                         "frac": round(value * 1e9 / ws / int_cells_peak, 5),
+                         "peak_dpx_instr_per_s": dpx, "peak_i32_instr_per_s": i32,
+                         "model": "4 DPX int16x2 instructions per cell (probe measured live)"},
+        "clocks": clk,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        sample = cpu_sample(wl, args.cpu_seconds, nthreads)
+        dt, cells, kind, desc = cpu_score(sample, wl, nthreads)
+        result["cpu_baseline"] = {"value": round(cells / dt / 1e9, 4), "unit": UNIT,
+                                  "cores": nthreads, "kind": kind,
+                                  "sample": f"{sample.n} of the {n} pairs (same seeded workload), "
+                                            f"{desc}, {cpu_isa()}",
+                                  "seconds": round(dt, 2)}
+    bsw.close()
+    dist.close()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+# -------------------------------------------------------------------- reference arm
+def run_reference(args):
+    from tal_bsw import synth
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    wl = synth.WORKLOADS[args.workload]
+    nthreads = os.cpu_count() or 1
+    # each step: a bounded sample of the workload, a few seconds of CPU work
+    per_step = max(1.0, min(6.0, 150.0 / max(args.steps + args.warmup, 1)))
+    sample = cpu_sample(wl, per_step, nthreads)
+    for _ in range(args.warmup):
+        cpu_score(sample, wl, nthreads)
+    tot_t, tot_c = 0.0, 0
+    kind = desc = ""
+    for _ in range(args.steps):
+        dt, cells, kind, desc = cpu_score(sample, wl, nthreads)
+        tot_t += dt
+        tot_c += cells
+    value = tot_c / tot_t / 1e9
+    bits = 8 if wl.bits == 8 else 16
+    res = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(tot_t / args.steps * 1e3, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "int16",
+           "data": "synthetic (seeded generator, no dataset)", "impl": "reference",
+           "config": {"workload": f"{wl.name}: {wl.n_pairs} pairs, w={wl.w}, getScores{bits}; "
+                                  f"each step a {sample.n}-pair sample"},
+           "pairs_per_s": round(sample.n * args.steps / tot_t, 1),
+           "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nthreads, "kind": kind,
+                            "sample": f"{sample.n} pairs per step, {desc}, {cpu_isa()}"},
+           "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(res), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -113,6 +113,17 @@ int64_t tal_bsw_last_bad_pair(tal_bsw_handle h);
 /* Number of kernel launches this handle has issued (for accounting). */
 uint64_t tal_bsw_launch_count(tal_bsw_handle h);
 
+/* DP cells the last collected call computed (sum over rows of the band
+ * width the reference's vector kernel visits for each pair).  The reference's
+ * own counter, BandedPairWiseSW::SW_cells, is never incremented
+ * (bandedSWA.cpp:199). */
+uint64_t tal_bsw_last_cells(tal_bsw_handle h);
+
+/* Measurement utility, no counterpart in the reference: integer-pipe
+ * throughput of `device` in thread-instructions per second, for the
+ * roofline -- packed 16x2 add-max (DPX) and plain int32. */
+int tal_bsw_probe_int_peak(int device, double *dpx_per_s, double *i32_per_s);
+
 #ifdef __cplusplus
 }
 #endif

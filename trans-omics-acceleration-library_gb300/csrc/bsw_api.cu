@@ -54,6 +54,7 @@ struct tal_bsw_ctx {
     std::string last_error;
     int64_t last_bad = -1;
     uint64_t launches = 0;
+    uint64_t last_cells = 0;
     int pending_status = TAL_OK;
     int forced_K = 0;
 };
@@ -74,6 +75,7 @@ struct Ctrl {
     int counter;
     int flags;
     long long bad_index;
+    unsigned long long cells;
 };
 
 template <int K>
@@ -108,6 +110,7 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
     A.work_counter = &c->counter;
     A.err_flags = &c->flags;
     A.err_index = &c->bad_index;
+    A.cells = &c->cells;
     A.P = h->kp;
     const int K = pick_k(h, w_for_k, A.cols_cap);
     size_t wbytes = talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, K);
@@ -116,7 +119,7 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
     size_t smem = (size_t)wpb * wbytes;
     if (smem > h->smem_optin)
         return fail(h, TAL_EDOMAIN, "pair too long for the shared-memory row buffers");
-    Ctrl init = {0, 0, (long long)INT64_MAX};
+    Ctrl init = {0, 0, (long long)INT64_MAX, 0ull};
     cudaError_t e = cudaMemcpyAsync(c, &init, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(ctrl)");
     if (K == 1) e = launch_k<1>(h, A, wpb, smem);
@@ -131,6 +134,7 @@ int collect(tal_bsw_ctx *h) {
     cudaError_t e = cudaMemcpyAsync(&c, h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "scoring");
+    h->last_cells = c.cells;
     if (c.flags) {
         h->last_bad = c.bad_index;
         std::string why;
@@ -295,9 +299,78 @@ __global__ void caps_kernel(const talbsw::DevPair *p, int n, int *out) {
     }
 }
 
+// Integer-pipe throughput probes: 8 independent dependency chains per thread.
+__global__ void probe_dpx_kernel(int iters, unsigned *out) {
+    unsigned a[8];
+    const unsigned b = 0xffff0001u;
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = threadIdx.x * 0x00010003u + k;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = __viaddmax_s16x2(a[k], b, 0x00020002u + k);
+    }
+    unsigned r = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) r ^= a[k];
+    if (r == 0x12345678u) out[0] = r;
+}
+
+__global__ void probe_i32_kernel(int iters, int *out) {
+    int a[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = (int)threadIdx.x * 3 + k;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = max(a[k] + 1, k - (int)i);
+    }
+    int r = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) r ^= a[k];
+    if (r == 0x12345678) out[0] = r;
+}
+
 }  // namespace
 
 extern "C" {
+
+int tal_bsw_probe_int_peak(int device, double *dpx_per_s, double *i32_per_s) {
+    if (!dpx_per_s || !i32_per_s) return TAL_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return TAL_ENODEV;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return TAL_ENODEV;
+    unsigned *d = nullptr;
+    if (cudaMalloc(&d, 16) != cudaSuccess) return TAL_ENOMEM;
+    const int threads = 256, blocks = prop.multiProcessorCount * 8, iters = 8192;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_dpx = 1e30f, best_i32 = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        float ms;
+        cudaEventRecord(e0);
+        probe_dpx_kernel<<<blocks, threads>>>(iters, d);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep) best_dpx = std::min(best_dpx, ms);
+        cudaEventRecord(e0);
+        probe_i32_kernel<<<blocks, threads>>>(iters, reinterpret_cast<int *>(d));
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep) best_i32 = std::min(best_i32, ms);
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    if (e != cudaSuccess) return TAL_ECUDA;
+    const double ops = (double)blocks * threads * iters * 8.0;
+    *dpx_per_s = ops / (best_dpx * 1e-3);
+    // the i32 chain step is an add and a max: two instructions
+    *i32_per_s = 2.0 * ops / (best_i32 * 1e-3);
+    return TAL_OK;
+}
 
 int tal_bsw_scores_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t *d_ref,
                           size_t ref_bytes, const uint8_t *d_qer, size_t qer_bytes,
@@ -360,5 +433,7 @@ const char *tal_bsw_last_error(tal_bsw_handle h) { return h ? h->last_error.c_st
 int64_t tal_bsw_last_bad_pair(tal_bsw_handle h) { return h ? h->last_bad : -1; }
 
 uint64_t tal_bsw_launch_count(tal_bsw_handle h) { return h ? h->launches : 0; }
+
+uint64_t tal_bsw_last_cells(tal_bsw_handle h) { return h ? h->last_cells : 0; }
 
 }  // extern "C"

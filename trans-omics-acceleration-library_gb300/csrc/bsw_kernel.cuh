@@ -65,6 +65,7 @@ struct LaunchArgs {
     int bits;                // 8, 16 or 0 = per-pair routing
     int cols_cap, rows_cap;  // shared-memory row capacity per warp
     int *work_counter;       // next work item (dynamic scheduling)
+    unsigned long long *cells;  // optional: total DP cells computed
     int *err_flags;
     long long *err_index;
     KernelParams P;
@@ -319,6 +320,7 @@ __global__ void __launch_bounds__(128) bsw_warp_kernel(LaunchArgs A) {
         int maxScore = h0e, x = 0, y = 0, gscore = -1, max_off = 0, max_ie = 0;
         int beg = 0, end = ncol, nbeg = 0, nend = ncol;
         const uint32_t full = 0xffffffffu;
+        unsigned long long ncells = 0;
 
         for (int i = 0; i < nrow; i++) {
             const int i1 = wrapS(i + 1, is8);
@@ -368,6 +370,7 @@ __global__ void __launch_bounds__(128) bsw_warp_kernel(LaunchArgs A) {
             }
 
             // ---- the row, strip by strip
+            if (end > beg) ncells += (unsigned long long)(end - beg);
             int carryP = INT_MIN;      // max of P over earlier strips
             int hprev = h10init;       // H of the column left of the strip
             uint32_t key = 0;          // (H << 16) | (j + 1), row max, last j wins ties
@@ -513,6 +516,7 @@ __global__ void __launch_bounds__(128) bsw_warp_kernel(LaunchArgs A) {
             }
         }
         if (lane == 0) {
+            if (A.cells) atomicAdd(A.cells, ncells);
             pp->score = maxScore;
             pp->tle = x;
             pp->qle = y;

@@ -52,6 +52,9 @@ _SIGS = {
     "tal_bsw_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "tal_bsw_last_bad_pair": (ctypes.c_int64, [ctypes.c_void_p]),
     "tal_bsw_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "tal_bsw_last_cells": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "tal_bsw_probe_int_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_double)]),
 }
 
 
@@ -138,6 +141,11 @@ class BandedPairWiseSW:
     def launch_count(self) -> int:
         return int(self._lib.tal_bsw_launch_count(self._h))
 
+    @property
+    def last_cells(self) -> int:
+        """DP cells computed by the last collected call."""
+        return int(self._lib.tal_bsw_last_cells(self._h))
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._lib.tal_bsw_destroy(self._h)
@@ -170,3 +178,13 @@ class BandedPairWiseSW:
         rc = self._lib.tal_bsw_scores(self._h, pa.ctypes.data, _buf_ptr(seqBufRef),
                                       _buf_ptr(seqBufQer), n, int(w), int(bits))
         self._check(rc)
+
+
+def probe_int_peak(device: int = 0):
+    """(DPX 16x2 add-max, int32) thread-instructions per second on `device`."""
+    lib = core_lib()
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = lib.tal_bsw_probe_int_peak(int(device), ctypes.byref(a), ctypes.byref(b))
+    if rc != TAL_OK:
+        raise TalBswError(rc, "tal_bsw_probe_int_peak failed")
+    return a.value, b.value
