@@ -124,6 +124,30 @@ uint64_t tal_bsw_last_cells(tal_bsw_handle h);
  * roofline -- packed 16x2 add-max (DPX) and plain int32. */
 int tal_bsw_probe_int_peak(int device, double *dpx_per_s, double *i32_per_s);
 
+/* Size in bytes of the library's fixed device scratch array used by
+ * tal_bsw_scores_device_noalloc (one per device, held until process exit). */
+#define TAL_BSW_NOALLOC_SCRATCH_BYTES 256
+
+/* Allocation-free scoring; no counterpart in the reference, which allocates
+ * its SIMD scratch inside every call (bandedSWA.cpp:2702-2703).
+ *
+ * For callers that must not allocate device memory while scoring (device
+ * memory owned by their own pool, or hot paths where cudaMalloc/cudaFree
+ * would synchronise the device).  Scores numPairs SeqPair records already in
+ * device memory, like tal_bsw_scores_device, but needs no handle and calls no
+ * allocator: its only scratch is a fixed TAL_BSW_NOALLOC_SCRATCH_BYTES device
+ * array inside the library (a control block), and a call whose scratch would
+ * not fit is refused with TAL_EDOMAIN.  Runs on `stream` (a cudaStream_t,
+ * NULL = default stream) of the current device and returns when the scores
+ * are in d_pairs.  The first call on each device resolves the scratch array's
+ * device address; make that first call before any stream capture.  All calls
+ * on a device share the one array and clear it themselves, so calls that
+ * overlap on the GPU (other threads or streams) race: serialise them. */
+int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_seq_pair *d_pairs,
+                                  const uint8_t *d_ref, size_t ref_bytes,
+                                  const uint8_t *d_qer, size_t qer_bytes, int32_t numPairs,
+                                  int32_t w, const int32_t *d_w, int bits, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,66 @@
+"""The allocation-free entry point (tal_bsw_scores_device_noalloc), called
+through the C ABI: two calls in a row on device buffers the test owns, each
+compared with the regular entry point (tal_bsw_scores) on the same pairs.
+Integer outputs, so the tolerance is zero.  Collected last on purpose."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import tal_bsw
+from tal_bsw import synth
+from tal_bsw.seqpair import outputs
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(lib, P, d_pairs, d_ref, d_qer, n, w, bits):
+    prm = tal_bsw.api._Params(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                              P["end_bonus"], P["a"], P["b"])
+    f = lib.tal_bsw_scores_device_noalloc
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                  ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32, ctypes.c_int32,
+                  ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    return f(ctypes.byref(prm), d_pairs.data_ptr(), d_ref.data_ptr(), d_ref.numel(),
+             d_qer.data_ptr(), d_qer.numel(), n, w, None, bits, None)
+
+
+@pytest.mark.parametrize("name,bits", [("c2_16bit", 16), ("c1_8bit", 8), ("c3_mixed", 0)])
+def test_noalloc_matches_regular_entry_point(name, bits):
+    import torch
+    wl = synth.WORKLOADS[name]
+    b = synth.generate(wl, 2000)
+    P = wl.params()
+    w = 100
+    expected = b.pairs.copy()
+    with tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                  P["end_bonus"], None, P["a"], P["b"], 1, device=0) as bsw:
+        bsw._scores(expected, b.ref, b.qer, b.n, w, bits)
+    lib = tal_bsw.api.core_lib()
+    torch.cuda.set_device(0)
+    d_ref = torch.from_numpy(b.ref).cuda()
+    d_qer = torch.from_numpy(b.qer).cuda()
+    for call in range(2):
+        d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
+        torch.cuda.synchronize()
+        rc = _noalloc(lib, P, d_pairs, d_ref, d_qer, b.n, w, bits)
+        assert rc == tal_bsw.api.TAL_OK, f"call {call}: status {rc}"
+        got = d_pairs.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE)
+        e, g = outputs(expected), outputs(got)
+        bad = np.nonzero((e != g).any(axis=1))[0]
+        assert bad.size == 0, f"call {call}: {bad.size} pairs differ, first {bad[0]}"
+
+
+def test_noalloc_reports_out_of_range_pairs():
+    import torch
+    b = synth.generate(synth.C1, 64)     # 151 bp: outside the 8-bit range
+    P = synth.C1.params()
+    lib = tal_bsw.api.core_lib()
+    d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
+    d_ref = torch.from_numpy(b.ref).cuda()
+    d_qer = torch.from_numpy(b.qer).cuda()
+    assert _noalloc(lib, P, d_pairs, d_ref, d_qer, b.n, 100, 8) == tal_bsw.api.TAL_EDOMAIN
+    # the next call clears the shared control block and succeeds
+    d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
+    assert _noalloc(lib, P, d_pairs, d_ref, d_qer, b.n, 100, 16) == tal_bsw.api.TAL_OK
