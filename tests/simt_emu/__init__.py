@@ -15,7 +15,7 @@ _lib = None
 
 def build(force=False):
     srcs = [os.path.join(HERE, "emu.cpp"), os.path.join(HERE, "fake", "cuda_runtime.h"),
-            os.path.join(CSRC, "bsw_kernel.cuh")]
+            os.path.join(CSRC, "bsw_kernel.cuh"), os.path.join(CSRC, "bsw_lane.cuh")]
     if force or not os.path.exists(SO) or os.path.getmtime(SO) < max(os.path.getmtime(s) for s in srcs):
         os.makedirs(os.path.dirname(SO), exist_ok=True)
         subprocess.check_call(["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-pthread", "-w",
@@ -24,7 +24,7 @@ def build(force=False):
     return SO
 
 
-def run(pairs, ref, qer, w, params, bits=16, K=4, warps=1, wpair=None):
+def run(pairs, ref, qer, w, params, bits=16, K=4, warps=1, wpair=None, G=32):
     """Scores a copy of pairs with the emulated kernel; returns (pairs, err_flags, err_index)."""
     global _lib
     if _lib is None:
@@ -43,5 +43,5 @@ def run(pairs, ref, qer, w, params, bits=16, K=4, warps=1, wpair=None):
                      ctypes.c_longlong(ref.shape[0]), vp(qer.ctypes.data), ctypes.c_longlong(0),
                      ctypes.c_longlong(qer.shape[0]), int(out.shape[0]), int(w),
                      None if wp is None else vp(wp.ctypes.data), int(bits), vp(kp.ctypes.data),
-                     int(K), int(warps), ctypes.byref(ef), ctypes.byref(ei))
+                     int(G), int(K), int(warps), ctypes.byref(ef), ctypes.byref(ei))
     return out, ef.value, ei.value

@@ -18,11 +18,13 @@ std::mutex atomic_mu;
 // The kernel's dynamic shared memory resolves to the per-block buffer.
 #define TALBSW_DYNAMIC_SMEM(name) unsigned char *name = simt::tl_smem
 #include "bsw_kernel.cuh"
+#include "bsw_lane.cuh"
+#include <functional>
 
 extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long ref_lo,
                            long long ref_hi, const uint8_t *qer, long long qer_lo,
                            long long qer_hi, int n, int w, const int32_t *wpair, int bits,
-                           const int32_t *kp, int K, int warps, int *err_flags,
+                           const int32_t *kp, int G, int K, int warps, int *err_flags,
                            long long *err_index) {
     talbsw::LaunchArgs A;
     std::memset(&A, 0, sizeof(A));
@@ -38,17 +40,18 @@ extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long
     *err_flags = 0; *err_index = (long long)INT64_MAX;
     A.work_counter = &counter; A.err_flags = err_flags; A.err_index = err_index;
     A.P = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], kp[6], kp[7]};
-    size_t wbytes = talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, K);
+    size_t wbytes = G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap)
+                           : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G);
     std::vector<unsigned char> smem(wbytes * warps + 64, 0xA5);  // poisoned, like fresh smem
     // warps run one after another; the 32 lanes of a warp are fibers
     int divergent = 0;
     for (int wi = 0; wi < warps; wi++) {
         simt::Warp *W = new simt::Warp();
         std::vector<std::vector<char>> stacks(32, std::vector<char>(1 << 18));
-        struct Arg { int t; simt::Warp *W; const talbsw::LaunchArgs *A; int K; unsigned char *sm; int warps; };
+        struct Arg { int t; simt::Warp *W; const talbsw::LaunchArgs *A; int G, K; unsigned char *sm; int warps; };
         static thread_local Arg args[32];
         for (int l = 0; l < 32; l++) {
-            args[l] = Arg{wi * 32 + l, W, &A, K, smem.data(), warps};
+            args[l] = Arg{wi * 32 + l, W, &A, G, K, smem.data(), warps};
             getcontext(&W->lane_ctx[l]);
             W->lane_ctx[l].uc_stack.ss_sp = stacks[l].data();
             W->lane_ctx[l].uc_stack.ss_size = stacks[l].size();
@@ -61,9 +64,17 @@ extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long
                 simt::tl_gridDim.x = 1;
                 simt::tl_warp = a.W;
                 simt::tl_smem = a.sm;
-                if (a.K == 1) talbsw::bsw_warp_kernel<1>(*a.A);
-                else if (a.K == 2) talbsw::bsw_warp_kernel<2>(*a.A);
-                else talbsw::bsw_warp_kernel<4>(*a.A);
+                if (a.G == 1) { talbsw::bsw_lane_kernel<0>(*a.A); a.W->done[a.t & 31] = true; return; }
+                switch (a.G * 10 + a.K) {
+                    case 44: talbsw::bsw_kernel<4, 4>(*a.A); break;
+                    case 42: talbsw::bsw_kernel<4, 2>(*a.A); break;
+                    case 84: talbsw::bsw_kernel<8, 4>(*a.A); break;
+                    case 82: talbsw::bsw_kernel<8, 2>(*a.A); break;
+                    case 164: talbsw::bsw_kernel<16, 4>(*a.A); break;
+                    case 162: talbsw::bsw_kernel<16, 2>(*a.A); break;
+                    case 322: talbsw::bsw_kernel<32, 2>(*a.A); break;
+                    default: talbsw::bsw_kernel<32, 4>(*a.A); break;
+                }
                 a.W->done[a.t & 31] = true;
             }, 1, l);
         }

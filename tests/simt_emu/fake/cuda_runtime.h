@@ -71,15 +71,25 @@ inline void gather(int64_t v, int64_t out[32]) {
 #define gridDim (simt::tl_gridDim)
 
 template <typename T>
-inline T __shfl_sync(unsigned, T v, int src) {
-    return (T)simt::exchange((int64_t)v, src & 31);
+inline T __shfl_sync(unsigned, T v, int src, int width = 32) {
+    int l = simt::lane();
+    int base = (l / width) * width;
+    return (T)simt::exchange((int64_t)v, base + (src % width));
 }
 template <typename T>
-inline T __shfl_up_sync(unsigned, T v, unsigned d) {
+inline T __shfl_up_sync(unsigned, T v, unsigned d, int width = 32) {
     int l = simt::lane();
+    int base = (l / width) * width;
     int src = l - (int)d;
-    T r = (T)simt::exchange((int64_t)v, src < 0 ? l : src);
-    return r;
+    return (T)simt::exchange((int64_t)v, src < base ? l : src);
+}
+template <typename T>
+inline T __shfl_xor_sync(unsigned, T v, int m, int width = 32) {
+    int l = simt::lane();
+    int base = (l / width) * width;
+    int src = l ^ m;
+    if (src < base || src >= base + width) src = l;
+    return (T)simt::exchange((int64_t)v, src);
 }
 inline unsigned __ballot_sync(unsigned, int pred) {
     int64_t all[32];
@@ -133,3 +143,12 @@ template <typename T, typename V>
 inline T atomicMin(T *p, V vv) { T v = (T)vv; std::lock_guard<std::mutex> g(simt::atomic_mu); T o = *p; if (v < o) *p = v; return o; }
 template <typename T, typename V>
 inline T atomicMax(T *p, V vv) { T v = (T)vv; std::lock_guard<std::mutex> g(simt::atomic_mu); T o = *p; if (v > o) *p = v; return o; }
+struct int2 { int x, y; };
+struct int4 { int x, y, z, w; };
+inline int2 make_int2(int a, int b) { return int2{a, b}; }
+inline int4 make_int4(int a, int b, int c, int d) { return int4{a, b, c, d}; }
+// DPX integer min/max (sm_90+): semantics per the CUDA math API
+inline int __viaddmin_s32(int a, int b, int c) { int s = a + b; return s < c ? s : c; }
+inline int __viaddmax_s32(int a, int b, int c) { int s = a + b; return s > c ? s : c; }
+inline int __viaddmax_s32_relu(int a, int b, int c) { int s = a + b; int m = s > c ? s : c; return m > 0 ? m : 0; }
+inline int __vimax3_s32(int a, int b, int c) { int m = a > b ? a : b; return m > c ? m : c; }

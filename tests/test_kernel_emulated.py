@@ -13,6 +13,7 @@ from tal_bsw.seqpair import outputs
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 FILES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+CONFIGS = [(1, 4), (4, 4), (8, 4), (8, 2), (16, 4), (32, 4), (32, 2), (4, 2), (16, 2)]
 
 
 @pytest.mark.parametrize("f", FILES, ids=os.path.basename)
@@ -23,12 +24,13 @@ def test_emulated_kernel_matches_golden(f):
     p = d["inputs"][:n]
     w = d["w"]
     bits = int(d["bits"])
-    K = (1, 2, 4)[sum(os.path.basename(f).encode()) % 3]
+    G, K = CONFIGS[sum(os.path.basename(f).encode()) % len(CONFIGS)]
     if np.ndim(w):
-        got, ef, _ = simt_emu.run(p, d["ref"], d["qer"], 0, P, bits=bits, K=K, wpair=w[:n])
+        got, ef, _ = simt_emu.run(p, d["ref"], d["qer"], 0, P, bits=bits, K=K, G=G, warps=2,
+                                  wpair=w[:n])
     else:
-        got, ef, _ = simt_emu.run(p, d["ref"], d["qer"], int(w), P, bits=bits, K=K)
+        got, ef, _ = simt_emu.run(p, d["ref"], d["qer"], int(w), P, bits=bits, K=K, G=G, warps=2)
     assert ef == 0
     e, g = outputs(d["expected"][:n]), outputs(got)
     bad = np.nonzero((e != g).any(1))[0]
-    assert bad.size == 0, f"K={K}: pair {bad[0]}: emu {g[bad[0]].tolist()} ref {e[bad[0]].tolist()}"
+    assert bad.size == 0, f"G={G} K={K}: pair {bad[0]}: emu {g[bad[0]].tolist()} ref {e[bad[0]].tolist()}"

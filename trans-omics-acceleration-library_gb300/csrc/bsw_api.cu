@@ -12,7 +12,7 @@
 #include <string>
 
 #include "../../include/tal_bsw.h"
-#include "bsw_kernel.cuh"
+#include "bsw_launch.cuh"
 
 static_assert(sizeof(tal_seq_pair) == 56, "SeqPair is 14 x int32 (bandedSWA.h:90-99)");
 static_assert(sizeof(talbsw::DevPair) == 56, "device SeqPair view");
@@ -56,7 +56,6 @@ struct tal_bsw_ctx {
     uint64_t launches = 0;
     uint64_t last_cells = 0;
     int pending_status = TAL_OK;
-    int forced_K = 0;
 };
 
 namespace {
@@ -78,32 +77,6 @@ struct Ctrl {
     unsigned long long cells;
 };
 
-template <int K>
-cudaError_t launch_k(tal_bsw_ctx *h, const talbsw::LaunchArgs &A, int wpb, size_t smem) {
-    auto kern = talbsw::bsw_warp_kernel<K>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    int bps = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, smem);
-    if (e != cudaSuccess) return e;
-    if (bps < 1) return cudaErrorInvalidConfiguration;
-    long long blocks = (long long)bps * h->num_sms;
-    long long need = ((long long)A.n + wpb - 1) / wpb;
-    if (blocks > need) blocks = std::max<long long>(need, 1);
-    kern<<<(unsigned)blocks, 32 * wpb, smem, h->stream>>>(A);
-    h->launches++;
-    return cudaGetLastError();
-}
-
-int pick_k(tal_bsw_ctx *h, int w, int cols_cap) {
-    if (h->forced_K == 1 || h->forced_K == 2 || h->forced_K == 4) return h->forced_K;
-    long long band = std::min<long long>(2LL * std::max(w, 0) + 1, (long long)cols_cap);
-    if (band <= 40) return 1;
-    if (band <= 100) return 2;
-    return 4;
-}
-
 // Issues the scoring launch for pairs already on the device.
 int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
     Ctrl *c = reinterpret_cast<Ctrl *>(h->ctrl.p);
@@ -112,19 +85,14 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
     A.err_index = &c->bad_index;
     A.cells = &c->cells;
     A.P = h->kp;
-    const int K = pick_k(h, w_for_k, A.cols_cap);
-    size_t wbytes = talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, K);
-    int wpb = 4;
-    while (wpb > 1 && (size_t)wpb * wbytes * 2 > h->smem_optin) wpb >>= 1;
-    size_t smem = (size_t)wpb * wbytes;
-    if (smem > h->smem_optin)
+    const talbsw::KConfig cfg = talbsw::choose_config(w_for_k, A.cols_cap);
+    if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap) > h->smem_optin)
         return fail(h, TAL_EDOMAIN, "pair too long for the shared-memory row buffers");
     Ctrl init = {0, 0, (long long)INT64_MAX, 0ull};
     cudaError_t e = cudaMemcpyAsync(c, &init, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(ctrl)");
-    if (K == 1) e = launch_k<1>(h, A, wpb, smem);
-    else if (K == 2) e = launch_k<2>(h, A, wpb, smem);
-    else e = launch_k<4>(h, A, wpb, smem);
+    e = talbsw::launch_config(A, cfg, h->num_sms, h->smem_optin, h->stream);
+    h->launches++;
     if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
     return TAL_OK;
 }
@@ -177,7 +145,6 @@ int tal_bsw_create(const tal_bsw_params *params, int device, tal_bsw_handle *out
     h->device = dev;
     h->num_sms = prop.multiProcessorCount;
     h->smem_optin = prop.sharedMemPerBlockOptin;
-    if (const char *k = getenv("TAL_BSW_K")) h->forced_K = atoi(k);
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = h->ctrl.ensure(sizeof(Ctrl));
     if (e != cudaSuccess) {

@@ -1,13 +1,16 @@
-// Banded Smith-Waterman seed extension on sm_103a: one warp per pair,
-// row-synchronous, each lane owning K consecutive columns of a 32*K-column
-// strip of the current row.
+// Banded Smith-Waterman seed extension on sm_103a: G lanes per pair (32/G
+// pairs per warp), row-synchronous, each lane owning K consecutive columns of
+// a G*K-column strip of the current row.
 //
 // Semantics: the reference's getScores16 / getScores8 kernels
 // (src/alignment/BSW/bandedSWA.cpp:2962-3356 / :2263-2661) for a pair scored on
 // its own.  Their outputs do not depend on which other pairs share the SIMD
 // group (checked against the reference on every workload shape), so a pair is
 // the unit of work here and the per-lane head/tail bookkeeping of the vector
-// code collapses to per-pair scalars held uniformly by the warp.
+// code collapses to per-pair scalars held uniformly by the pair's G lanes.
+// Several pairs share a warp so that this per-row bookkeeping (band edges,
+// narrowing, z-drop) is paid once per warp-instruction for 32/G pairs; each
+// group takes its next pair from the work counter as soon as it finishes.
 //
 // Per row i the reference computes, over its band [beg, end):
 //   M(j)   = H(i-1,j-1) ? H(i-1,j-1) + S(i,j) : 0
@@ -22,9 +25,14 @@
 // reduction, so a whole strip is one pass with no serial dependency.
 //
 // The row buffers live in shared memory, one per warp, exactly as the
-// reference's scratch rows: HF[j] packs H_h[j] (low 16 bits) and F[j] (high 16
-// bits); columns outside the computed band keep their old ("stale") values,
-// which the reference's narrowing reads.
+// reference's scratch rows H_h[j] and F[j] (int32 each); columns outside the
+// computed band keep their old ("stale") values, which the reference's
+// narrowing reads.
+//
+// A row is cut into strips of G*K columns, each lane owning K consecutive
+// columns.  All collectives (shuffles, ballots) run with the full warp mask in
+// warp-uniform loops; a group with nothing to do in an iteration is masked by
+// predicates, never by divergence around a collective.
 #pragma once
 
 #include <stdint.h>
@@ -63,7 +71,7 @@ struct LaunchArgs {
     int32_t n;
     int32_t w;
     int bits;                // 8, 16 or 0 = per-pair routing
-    int cols_cap, rows_cap;  // shared-memory row capacity per warp
+    int cols_cap, rows_cap;  // shared-memory row capacity per pair
     int *work_counter;       // next work item (dynamic scheduling)
     unsigned long long *cells;  // optional: total DP cells computed
     int *err_flags;
@@ -71,38 +79,13 @@ struct LaunchArgs {
     KernelParams P;
 };
 
-// Element-width wrap helpers: the reference's per-row bookkeeping is int16
-// (or int8) arithmetic that wraps; it is emulated exactly.
-__device__ __forceinline__ int wrapS(int x, bool is8) {
-    return is8 ? (int)(int8_t)x : (int)(int16_t)x;
-}
-__device__ __forceinline__ int wrapU(int x, bool is8) {
-    return is8 ? (int)(uint8_t)x : (int)(uint16_t)x;
-}
+// Element-width wrap of the reference's per-row int16 / int8 arithmetic,
+// emulated exactly: sh = 16 (int16) or 24 (int8), msk = 0xffff or 0xff.
+__device__ __forceinline__ int wrapS(int x, int sh) { return (int)((unsigned)x << sh) >> sh; }
+__device__ __forceinline__ int wrapU(int x, int msk) { return x & msk; }
 
 __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
 __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
-
-// first non-zero word of HF in [lo, hi) scanning up; hi if none
-__device__ __forceinline__ int scan_first_nz(const uint32_t *HF, int lo, int hi, int lane) {
-    for (int b = lo; b < hi; b += 32) {
-        int j = b + lane;
-        bool nz = (j < hi) && HF[j] != 0u;
-        unsigned m = __ballot_sync(0xffffffffu, nz);
-        if (m) return b + __ffs(m) - 1;
-    }
-    return hi;
-}
-// last non-zero word of HF in [lo, hi] scanning down from hi; lo-1 if none
-__device__ __forceinline__ int scan_last_nz(const uint32_t *HF, int lo, int hi, int lane) {
-    for (int t = hi; t >= lo; t -= 32) {
-        int j = t - lane;
-        bool nz = (j >= lo) && HF[j] != 0u;
-        unsigned m = __ballot_sync(0xffffffffu, nz);
-        if (m) return t - (__ffs(m) - 1);
-    }
-    return lo - 1;
-}
 
 // Can this pair be scored exactly with the 8-bit (is8) or 16-bit rules?
 // The per-cell arithmetic runs in int32, which equals the reference's
@@ -133,57 +116,74 @@ template <int K>
 struct VecIO;
 template <>
 struct VecIO<1> {
-    __device__ static void ld(const uint32_t *p, uint32_t (&v)[1]) { v[0] = p[0]; }
-    __device__ static void st(uint32_t *p, const uint32_t (&v)[1]) { p[0] = v[0]; }
-    __device__ static uint32_t ldq(const uint8_t *q) { return q[0]; }
+    __device__ static void ld(const int *p, int (&v)[1]) { v[0] = p[0]; }
+    __device__ static void st(int *p, const int (&v)[1]) { p[0] = v[0]; }
+    __device__ static void ldq(const uint16_t *q, uint32_t (&v)[1]) { v[0] = q[0]; }
 };
 template <>
 struct VecIO<2> {
-    __device__ static void ld(const uint32_t *p, uint32_t (&v)[2]) {
-        uint2 t = *reinterpret_cast<const uint2 *>(p);
+    __device__ static void ld(const int *p, int (&v)[2]) {
+        int2 t = *reinterpret_cast<const int2 *>(p);
         v[0] = t.x; v[1] = t.y;
     }
-    __device__ static void st(uint32_t *p, const uint32_t (&v)[2]) {
-        *reinterpret_cast<uint2 *>(p) = make_uint2(v[0], v[1]);
+    __device__ static void st(int *p, const int (&v)[2]) {
+        *reinterpret_cast<int2 *>(p) = make_int2(v[0], v[1]);
     }
-    __device__ static uint32_t ldq(const uint8_t *q) {
-        return *reinterpret_cast<const uint16_t *>(q);
+    __device__ static void ldq(const uint16_t *q, uint32_t (&v)[2]) {
+        uint32_t w = *reinterpret_cast<const uint32_t *>(q);
+        v[0] = w; v[1] = w >> 16;   // PRMT reads only the low 16 bits of a selector
     }
 };
 template <>
 struct VecIO<4> {
-    __device__ static void ld(const uint32_t *p, uint32_t (&v)[4]) {
-        uint4 t = *reinterpret_cast<const uint4 *>(p);
+    __device__ static void ld(const int *p, int (&v)[4]) {
+        int4 t = *reinterpret_cast<const int4 *>(p);
         v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
     }
-    __device__ static void st(uint32_t *p, const uint32_t (&v)[4]) {
-        *reinterpret_cast<uint4 *>(p) = make_uint4(v[0], v[1], v[2], v[3]);
+    __device__ static void st(int *p, const int (&v)[4]) {
+        *reinterpret_cast<int4 *>(p) = make_int4(v[0], v[1], v[2], v[3]);
     }
-    __device__ static uint32_t ldq(const uint8_t *q) {
-        return *reinterpret_cast<const uint32_t *>(q);
+    __device__ static void ldq(const uint16_t *q, uint32_t (&v)[4]) {
+        uint2 w = *reinterpret_cast<const uint2 *>(q);
+        v[0] = w.x; v[1] = w.x >> 16; v[2] = w.y; v[3] = w.y >> 16;
     }
 };
 
-// Shared-memory footprint of one warp's rows, in bytes (16-byte aligned parts).
-__host__ __device__ __forceinline__ size_t warp_smem_bytes(int cols_cap, int rows_cap, int K) {
-    size_t hf = ((size_t)(cols_cap + 2 + K) * 4 + 15) & ~(size_t)15;
-    size_t q = ((size_t)(cols_cap + K + 16) + 15) & ~(size_t)15;
+constexpr int KPAD = 4;  // widest strip's columns per lane: row padding
+
+// Shared-memory footprint of one pair's rows, in bytes (16-byte aligned parts):
+// H_h and F (int32 each), the query as 16-bit byte-permute selectors, the
+// target as base codes.
+__host__ __device__ __forceinline__ size_t smem_hh_bytes(int cols_cap) {
+    return ((size_t)(cols_cap + 2 + KPAD) * 4 + 15) & ~(size_t)15;
+}
+__host__ __device__ __forceinline__ size_t smem_q_bytes(int cols_cap) {
+    return ((size_t)(cols_cap + KPAD + 8) * 2 + 15) & ~(size_t)15;
+}
+__host__ __device__ __forceinline__ size_t pair_smem_bytes(int cols_cap, int rows_cap) {
     size_t t = ((size_t)(rows_cap + 16) + 15) & ~(size_t)15;
-    return hf + q + t;
+    return 2 * smem_hh_bytes(cols_cap) + smem_q_bytes(cols_cap) + t;
+}
+// one warp = 32/G pairs
+__host__ __device__ __forceinline__ size_t warp_smem_bytes(int cols_cap, int rows_cap, int G) {
+    return (size_t)(32 / G) * pair_smem_bytes(cols_cap, rows_cap);
 }
 
 // Stage len bytes at window offset `off` of the device window src (window
-// length buf_bytes, 16-byte aligned start) into shared dst as base codes,
-// with 16-byte vector loads; returns false (warp-uniform) if any byte is
-// above 4.
-__device__ __forceinline__ bool stage_bases(uint8_t *dst, const uint8_t *src, int len,
-                                            size_t buf_bytes, size_t off, int lane) {
+// length buf_bytes, 16-byte aligned start) into shared dst, G lanes sharing
+// the work (lane gl), with 16-byte vector loads; each base code b is stored as
+// b * MUL + ADD (the query as a ready-made byte-permute selector).
+// Returns true in a lane that saw a byte above 4.
+template <int G, typename T, uint32_t MUL, uint32_t ADD>
+__device__ __forceinline__ bool stage_bases(T *dst, const uint8_t *src, int len,
+                                            size_t buf_bytes, size_t off, int gl) {
+    bool bad = false;
+    if (len <= 0) return false;
     // aligned 16-byte chunks covering [off, off+len), never past the window
     size_t a0 = off & ~(size_t)15;
     size_t a1 = (off + (size_t)len + 15) & ~(size_t)15;
     if (a1 > (buf_bytes & ~(size_t)15)) a1 = buf_bytes & ~(size_t)15;
-    bool bad = false;
-    for (size_t c = a0 + (size_t)lane * 16; c < a1; c += 32 * 16) {
+    for (size_t c = a0 + (size_t)gl * 16; c < a1; c += (size_t)G * 16) {
         uint4 v = *reinterpret_cast<const uint4 *>(src + c);
         uint32_t wv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
@@ -192,339 +192,549 @@ __device__ __forceinline__ bool stage_bases(uint8_t *dst, const uint8_t *src, in
             if (pos >= off && pos < off + (size_t)len) {
                 uint32_t byte = (wv[b >> 2] >> ((b & 3) * 8)) & 0xffu;
                 if (byte > 4u) bad = true;
-                dst[pos - off] = (uint8_t)byte;
+                dst[pos - off] = (T)(byte * MUL + ADD);
             }
         }
     }
     // tail bytes past the last whole 16-byte unit of the buffer
     size_t done = a1 > off ? a1 - off : 0;
-    for (size_t p = done + lane; p < (size_t)len; p += 32) {
+    for (size_t p = done + gl; p < (size_t)len; p += G) {
         uint32_t byte = src[off + p];
         if (byte > 4u) bad = true;
-        dst[p] = (uint8_t)byte;
+        dst[p] = (T)(byte * MUL + ADD);
     }
-    return __any_sync(0xffffffffu, bad) == 0;
+    return bad;
 }
 
-template <int K>
-__global__ void __launch_bounds__(128) bsw_warp_kernel(LaunchArgs A) {
+constexpr int NEG = -(1 << 29);  // "minus infinity" for the E scan, no overflow
+
+// Byte permute with the PTX sign-replicate bit honoured: selector nibble
+// 8|q copies the sign of source byte q.  A query code q is stored as the
+// selector q*0x1111 + 0x8880, so the result is the score byte q of the row's
+// table, sign-extended to 32 bits.
+__device__ __forceinline__ int prmt_sext(uint32_t lo, uint32_t hi, uint32_t sel) {
+#if defined(__CUDA_ARCH__)
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(lo), "r"(hi), "r"(sel));
+    return (int)r;
+#else
+    const uint64_t v = ((uint64_t)hi << 32) | lo;
+    uint32_t r = 0;
+    for (int n = 0; n < 4; n++) {
+        const uint32_t c = (sel >> (4 * n)) & 0xfu;
+        uint32_t b = (uint32_t)(v >> (8 * (c & 7u))) & 0xffu;
+        if (c & 8u) b = (b & 0x80u) ? 0xffu : 0u;
+        r |= b << (8 * n);
+    }
+    return (int)r;
+#endif
+}
+
+// (hi16 of the result) = h, (lo16) = k: h << 16 | k for 0 <= h, k < 65536.
+__device__ __forceinline__ uint32_t pack_key(int h, uint32_t k) {
+    return __byte_perm(k, (uint32_t)h, 0x5410u);
+}
+
+// Constants of the cell recurrence.  The gap parameters are at most 127 and
+// o + e fits every pair routed to the 8-bit rules, so they need no wrap.
+struct CellConsts {
+    int e_ins, e_del, oe_del;
+    int ke[4];    // k * e_ins
+    int keoe[4];  // k * e_ins - oe_ins
+    int ce[4];    // -(k - 1) * e_ins
+    uint32_t kp1[4];  // k + 1
+};
+
+// Per-row state of one pair, shared by the strips of the row.
+struct RowState {
+    int beg, end, head, tail;
+    uint32_t tlo, thi;  // score table of the row's target base (signed bytes)
+    int carryP;         // max over columns left of the strip of P (units of (j - beg))
+    int hprev;          // H of the column left of the strip
+    int h10init;        // H(i, beg - 1): first-column value or 0
+    uint32_t key;       // lane's max of (H << 16) | (j + 1) over valid columns
+    int hlast;          // H(i, end - 1), held by the lane that owns the column
+};
+
+// Strip kinds, chosen warp-uniformly (the most general any pair needs):
+// interior strips lie inside [beg, end) and the head/tail window, edge strips
+// cross beg or end, masked strips also cross the head/tail window.
+enum { STRIP_INTERIOR = 0, STRIP_EDGE = 1, STRIP_MASKED = 2 };
+
+// One strip of a pair's row: columns [base, base + G*K), lane gl owning
+// [base + gl*K, +K).  `act` false: the pair has no strip here (no effects).
+template <int G, int K, int MODE>
+__device__ __forceinline__ void do_strip(const int base, const bool act, const int gl,
+                                         RowState &r, const CellConsts &c, int *Hh, int *Fv,
+                                         const uint16_t *Qs) {
+    const unsigned full = 0xffffffffu;
+    const int j0 = base + gl * K;
+    int hv[K], fv[K];
+    uint32_t qs[K];
+    const bool ld = act && (MODE == STRIP_INTERIOR || j0 < r.end);
+    if (ld) {
+        VecIO<K>::ld(Hh + j0, hv);
+        VecIO<K>::ld(Fv + j0, fv);
+        VecIO<K>::ldq(Qs + j0, qs);
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; k++) { hv[k] = 0; fv[k] = 0; qs[k] = 0x8880u; }
+    }
+    const int lo = r.beg - j0;  // columns k < lo lie left of the band
+    const int hi = r.end - j0;  // columns k >= hi lie right of it
+    // pass 1: M and the lane-local prefix of P'(k) = max(M - oe_ins, 0) + k*e_ins
+    int mm[K], lp[K];
+    int run = NEG;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int sb = prmt_sext(r.tlo, r.thi, qs[k]);               // S(t, q)
+        mm[k] = __viaddmin_s32(hv[k], sb, hv[k] << 12);              // h00 ? h00 + S : <= 0
+        int p = __viaddmax_s32(mm[k], c.keoe[k], c.ke[k]);
+        if (MODE != STRIP_INTERIOR && k < lo) p = NEG;
+        run = imax(run, p);
+        lp[k] = run;
+    }
+    // scan of the lane summaries across the pair's G lanes (units of (j - beg))
+    const int off = c.e_ins * (j0 - r.beg);
+    int incl = lp[K - 1] + off;
+#pragma unroll
+    for (int d = 1; d < G; d <<= 1) incl = imax(incl, __shfl_up_sync(full, incl, d, G));
+    int excl = __shfl_up_sync(full, incl, 1, G);
+    excl = (gl == 0) ? r.carryP : imax(excl, r.carryP);
+    const int ctot = __shfl_sync(full, incl, G - 1, G);
+    if (act) r.carryP = imax(r.carryP, ctot);
+    const int X = excl - off;
+    // pass 2: E and H
+    int H[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int R = (k == 0) ? X : imax(X, lp[k - 1]);
+        H[k] = __vimax3_s32(mm[k], R + c.ce[k], fv[k]);
+    }
+    int hl = __shfl_up_sync(full, H[K - 1], 1, G);
+    if (gl == 0) hl = r.hprev;
+    const int hnext = __shfl_sync(full, H[K - 1], G - 1, G);
+    if (act) r.hprev = hnext;   // a pair with no strip here keeps its last H
+    // pass 3: stores and the row maximum
+    int ho[K], fo[K];
+    uint32_t lkey = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        int hst = (k == 0) ? hl : H[k - 1];
+        int f2 = __viaddmax_s32_relu(fv[k], -c.e_del, mm[k] - c.oe_del);
+        uint32_t kk = pack_key(H[k], c.kp1[k]);
+        if (MODE != STRIP_INTERIOR) {
+            const bool in = k >= lo && k < hi;
+            if (k == lo) hst = r.h10init;
+            bool valid = in;
+            if (MODE == STRIP_MASKED) {
+                const int j = j0 + k;
+                if (j < r.head || j > r.tail) { hst = 0; f2 = 0; }
+                valid = in && j >= r.head && j < r.tail;
+            }
+            if (!valid) kk = 0;
+            if (k == hi - 1) r.hlast = H[k];
+        }
+        ho[k] = hst;
+        fo[k] = f2;
+        lkey = kk > lkey ? kk : lkey;
+    }
+    if (act) {
+        if (lkey) lkey += (uint32_t)j0;
+        r.key = lkey > r.key ? lkey : r.key;
+    }
+    if (ld) {
+        if (MODE == STRIP_INTERIOR || (lo <= 0 && hi >= K)) {
+            VecIO<K>::st(Hh + j0, ho);
+            VecIO<K>::st(Fv + j0, fo);
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                if (k >= lo && k < hi) {
+                    Hh[j0 + k] = ho[k];
+                    Fv[j0 + k] = fo[k];
+                }
+            }
+        }
+    }
+}
+
+// Max over a pair's G lanes.
+template <int G>
+__device__ __forceinline__ unsigned group_max(unsigned v) {
+    if constexpr (G == 32) {
+        return __reduce_max_sync(0xffffffffu, v);
+    } else {
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+            unsigned t = __shfl_xor_sync(0xffffffffu, v, o, G);
+            v = t > v ? t : v;
+        }
+        return v;
+    }
+}
+
+// First column of [lo, hi) with H_h | F non-zero, scanning up; hi if none.
+// Warp-uniform loop; each pair searches with its own G lanes.
+template <int G>
+__device__ __forceinline__ int scan_first_nz(const int *Hh, const int *Fv, int lo, int hi,
+                                             bool act, int gl, int gshift, unsigned gbits) {
+    int found = hi;
+    bool srch = act && lo < hi;
+    int b = lo;
+    while (__any_sync(0xffffffffu, srch)) {
+        const int j = b + gl;
+        const bool nz = srch && j < hi && ((Hh[j] | Fv[j]) != 0);
+        const unsigned m = (__ballot_sync(0xffffffffu, nz) & gbits) >> gshift;
+        if (srch) {
+            if (m) { found = b + __ffs(m) - 1; srch = false; }
+            else { b += G; if (b >= hi) srch = false; }
+        }
+    }
+    return found;
+}
+// Last column of [lo, hi] with H_h | F non-zero, scanning down; lo-1 if none.
+template <int G>
+__device__ __forceinline__ int scan_last_nz(const int *Hh, const int *Fv, int lo, int hi,
+                                            bool act, int gl, int gshift, unsigned gbits) {
+    int found = lo - 1;
+    bool srch = act && hi >= lo;
+    int t = hi;
+    while (__any_sync(0xffffffffu, srch)) {
+        const int j = t - gl;
+        const bool nz = srch && j >= lo && ((Hh[j] | Fv[j]) != 0);
+        const unsigned m = (__ballot_sync(0xffffffffu, nz) & gbits) >> gshift;
+        if (srch) {
+            if (m) { found = t - (__ffs(m) - 1); srch = false; }
+            else { t -= G; if (t < lo) srch = false; }
+        }
+    }
+    return found;
+}
+
+// Per-pair state, uniform across the pair's G lanes.
+struct PairState {
+    int pidx, nrow, ncol, i;
+    int beg, end, nbeg, nend, head, tail;
+    int maxScore, x, y, gscore, max_ie, max_off;
+    int h0e, o_delE, e_delE, bandE, wk, qlenE, mlen, zdropE;
+    int sh, msk;  // element width: wrap shift and unsigned mask
+    bool is8;
+    unsigned long long ncells;
+};
+
+template <int G, int K>
+__global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
     TALBSW_DYNAMIC_SMEM(smem_raw);
+    constexpr int NG = 32 / G;
+    constexpr int SPAN = G * K;
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    const size_t wbytes = warp_smem_bytes(A.cols_cap, A.rows_cap, K);
-    unsigned char *wbase = smem_raw + (size_t)wib * wbytes;
-    uint32_t *HF = reinterpret_cast<uint32_t *>(wbase);
-    uint8_t *Q = wbase + (((size_t)(A.cols_cap + 2 + K) * 4 + 15) & ~(size_t)15);
-    uint8_t *Tt = Q + (((size_t)(A.cols_cap + K + 16) + 15) & ~(size_t)15);
+    const int g = lane / G, gl = lane % G, gshift = g * G;
+    const unsigned gbits = (G == 32) ? full : (((1u << G) - 1u) << gshift);
+    const size_t pbytes = pair_smem_bytes(A.cols_cap, A.rows_cap);
+    unsigned char *pbase = smem_raw + ((size_t)wib * NG + g) * pbytes;
+    int *Hh = reinterpret_cast<int *>(pbase);
+    int *Fv = reinterpret_cast<int *>(pbase + smem_hh_bytes(A.cols_cap));
+    uint16_t *Qs = reinterpret_cast<uint16_t *>(pbase + 2 * smem_hh_bytes(A.cols_cap));
+    uint8_t *Tt = pbase + 2 * smem_hh_bytes(A.cols_cap) + smem_q_bytes(A.cols_cap);
     const KernelParams P = A.P;
-    const int span = 32 * K;
+
+    CellConsts cc;
+    cc.e_ins = P.e_ins;
+    cc.e_del = P.e_del;
+    cc.oe_del = P.o_del + P.e_del;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        cc.ke[k] = k * P.e_ins;
+        cc.keoe[k] = k * P.e_ins - (P.o_ins + P.e_ins);
+        cc.ce[k] = -(k - 1) * P.e_ins;
+        cc.kp1[k] = (uint32_t)(k + 1);
+    }
+    const int oe_ins = P.o_ins + P.e_ins;
+
+    PairState ps;
+    ps.pidx = 0; ps.nrow = 0; ps.ncol = 0; ps.i = 0; ps.ncells = 0;
+    bool active = false, done = false;
+
+    auto finish = [&]() {
+        if (gl == 0) {
+            DevPair *pp = A.pairs + ps.pidx;
+            if (A.cells) atomicAdd(A.cells, ps.ncells);
+            pp->score = ps.maxScore;
+            pp->tle = ps.x;
+            pp->qle = ps.y;
+            pp->max_off = ps.max_off;
+            pp->gscore = ps.gscore;
+            pp->gtle = ps.max_ie;
+        }
+        active = false;
+    };
 
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(A.work_counter, 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= A.n) break;
-        const int pidx = A.order ? A.order[item] : item;
-        DevPair *pp = A.pairs + pidx;
-        const int len1 = pp->len1, len2 = pp->len2, h0in = pp->h0;
-        const int idr = pp->idr, idq = pp->idq;
-        const int wcall = A.wpair ? A.wpair[pidx] : A.w;
-
-        // ---- precision routing and range checks (warp-uniform)
-        bool is8;
-        if (A.bits == 8) is8 = true;
-        else if (A.bits == 16) is8 = false;
-        else is8 = pair_in_range(P, len1, len2, h0in, wcall, true);
-        bool ok = pair_in_range(P, len1, len2, h0in, wcall, is8) && wcall >= 0;
-        ok = ok && (long long)idr >= A.ref_lo && (long long)idq >= A.qer_lo &&
-             (long long)idr + len1 <= A.ref_hi && (long long)idq + len2 <= A.qer_hi;
-        if (!ok) {
-            if (lane == 0) {
-                atomicOr(A.err_flags, ERR_DOMAIN);
-                atomicMin(A.err_index, (long long)pidx);
+        // ---- groups without a pair take the next one
+        const bool need = !active && !done;
+        if (__any_sync(full, need)) {
+            int item = 0;
+            if (need && gl == 0) item = atomicAdd(A.work_counter, 1);
+            item = __shfl_sync(full, item, gshift);
+            const bool take = need && item < A.n;
+            if (need && !take) done = true;
+            int len1 = 0, len2 = 0, h0in = 0, idr = 0, idq = 0, wcall = 0, pidx = 0;
+            bool is8 = false, ok = false;
+            if (take) {
+                pidx = A.order ? A.order[item] : item;
+                const DevPair *pp = A.pairs + pidx;
+                len1 = pp->len1; len2 = pp->len2; h0in = pp->h0;
+                idr = pp->idr; idq = pp->idq;
+                wcall = A.wpair ? A.wpair[pidx] : A.w;
+                if (A.bits == 8) is8 = true;
+                else if (A.bits == 16) is8 = false;
+                else is8 = pair_in_range(P, len1, len2, h0in, wcall, true);
+                ok = pair_in_range(P, len1, len2, h0in, wcall, is8) && wcall >= 0 &&
+                     (long long)idr >= A.ref_lo && (long long)idq >= A.qer_lo &&
+                     (long long)idr + len1 <= A.ref_hi && (long long)idq + len2 <= A.qer_hi;
+                if (!ok) {
+                    if (gl == 0) {
+                        atomicOr(A.err_flags, ERR_DOMAIN);
+                        atomicMin(A.err_index, (long long)pidx);
+                    }
+                } else if (len2 > A.cols_cap || len1 > A.rows_cap) {
+                    ok = false;
+                    if (gl == 0) {
+                        atomicOr(A.err_flags, ERR_CAPACITY);
+                        atomicMin(A.err_index, (long long)pidx);
+                    }
+                }
             }
-            continue;
-        }
-        if (len2 > A.cols_cap || len1 > A.rows_cap) {
-            if (lane == 0) {
-                atomicOr(A.err_flags, ERR_CAPACITY);
-                atomicMin(A.err_index, (long long)pidx);
+            bool st = take && ok;
+            // stage the bases (query as PRMT selectors)
+            bool bad = stage_bases<G, uint16_t, 0x1111u, 0x8880u>(
+                Qs, A.qer, st ? len2 : 0, (size_t)(A.qer_hi - A.qer_lo),
+                st ? (size_t)(idq - A.qer_lo) : 0, gl);
+            bad |= stage_bases<G, uint8_t, 1u, 0u>(
+                Tt, A.ref, st ? len1 : 0, (size_t)(A.ref_hi - A.ref_lo),
+                st ? (size_t)(idr - A.ref_lo) : 0, gl);
+            const unsigned bm = __ballot_sync(full, bad) & gbits;
+            if (st && bm) {
+                if (gl == 0) {
+                    atomicOr(A.err_flags, ERR_BASE);
+                    atomicMin(A.err_index, (long long)pidx);
+                }
+                st = false;
             }
-            continue;
-        }
-        const int ncol = len2, nrow = len1;
-
-        // ---- stage bases (codes 0..4) into shared memory
-        bool gq = stage_bases(Q, A.qer, len2, (size_t)(A.qer_hi - A.qer_lo),
-                              (size_t)(idq - A.qer_lo), lane);
-        bool gt = stage_bases(Tt, A.ref, len1, (size_t)(A.ref_hi - A.ref_lo),
-                              (size_t)(idr - A.ref_lo), lane);
-        if (!(gq && gt)) {
-            if (lane == 0) {
-                atomicOr(A.err_flags, ERR_BASE);
-                atomicMin(A.err_index, (long long)pidx);
+            if (st) {
+                // per-pair constants (smithWatermanBatchWrapper16/8 set-up)
+                const int sh = is8 ? 24 : 16, msk = is8 ? 0xff : 0xffff;
+                ps.is8 = is8; ps.sh = sh; ps.msk = msk;
+                ps.pidx = pidx; ps.nrow = len1; ps.ncol = len2; ps.i = 0; ps.ncells = 0;
+                ps.h0e = wrapS(wrapU(h0in, msk), sh);
+                ps.o_delE = P.o_del;
+                ps.e_delE = P.e_del;
+                int maxsc = 0;  // max(0, a, -b, -1) in the element type (:2779-2782)
+                {
+                    int av = wrapS((int8_t)P.a, sh), bv = wrapS((int8_t)(-P.b), sh);
+                    if (maxsc < av) maxsc = av;
+                    if (maxsc < bv) maxsc = bv;
+                    if (maxsc < -1) maxsc = -1;
+                }
+                // band clamp (:2882-2904): integer division, then +1
+                int myband;
+                {
+                    const int qlen_b = wrapU(len2 * maxsc, msk);
+                    const int tmp1 = wrapU(qlen_b + wrapS(P.end_bonus - P.o_ins, sh), msk);
+                    int mi = tmp1 / P.e_ins + 1;
+                    if (mi < 1) mi = 1;
+                    myband = wrapU(wcall > mi ? mi : wcall, msk);
+                    const int tmp2 = wrapU(qlen_b + wrapS(P.end_bonus - P.o_del, sh), msk);
+                    int md = tmp2 / P.e_del + 1;
+                    if (md < 1) md = 1;
+                    myband = wrapU(myband > md ? md : myband, msk);
+                    ps.wk = wcall < myband ? myband : wcall;
+                }
+                ps.qlenE = wrapS(len2, sh);
+                const int tlenE = wrapS(len1, sh);
+                ps.mlen = wrapS(imin(wrapU(ps.qlenE + myband, msk), wrapU(tlenE, msk)), sh);
+                ps.zdropE = wrapS(P.zdrop, sh);
+                ps.bandE = wrapS(myband, sh);
+                ps.head = 0; ps.tail = ps.qlenE;
+                ps.maxScore = ps.h0e; ps.x = 0; ps.y = 0; ps.gscore = -1; ps.max_off = 0;
+                ps.max_ie = 0;
+                ps.beg = 0; ps.end = len2; ps.nbeg = 0; ps.nend = len2;
+                // row 0 values H_h[k] and F[k] = 0 (:2839-2879)
+                const int v1 = (ps.h0e > oe_ins) ? wrapS(ps.h0e - oe_ins, sh) : 0;
+                const int top = len2 > 1 ? len2 : 1;
+                for (int k = gl; k <= top; k += G) {
+                    int hv;
+                    if (k == 0) hv = ps.h0e;
+                    else if (k == 1) hv = v1;
+                    else if (k < len2) hv = imax(v1 - (k - 1) * P.e_ins, 0);
+                    else hv = 0;
+                    Hh[k] = hv;
+                    Fv[k] = 0;
+                }
+                active = true;
             }
             __syncwarp();
-            continue;
         }
+        if (__all_sync(full, done)) break;
 
-        // ---- per-pair constants (smithWatermanBatchWrapper16/8 set-up)
-        const int h0e = wrapS(wrapU(h0in, is8), is8);
-        const int oe_insE = wrapS(P.o_ins + P.e_ins, is8);
-        const int e_insE = wrapS(P.e_ins, is8), e_delE = wrapS(P.e_del, is8);
-        const int o_delE = wrapS(P.o_del, is8);
-        int maxsc = 0;  // max(0, a, -b, -1) in the element type (:2779-2782)
-        {
-            int av = wrapS((int8_t)P.a, is8), bv = wrapS((int8_t)(-P.b), is8);
-            if (maxsc < av) maxsc = av;
-            if (maxsc < bv) maxsc = bv;
-            if (maxsc < -1) maxsc = -1;
-        }
-        // band clamp (:2882-2904): integer division, then +1
-        int myband, wk;
-        {
-            const int qlen_b = wrapU(len2 * maxsc, is8);
-            const int tmp1 = wrapU(qlen_b + wrapS(P.end_bonus - P.o_ins, is8), is8);
-            int mi = tmp1 / P.e_ins + 1;
-            if (mi < 1) mi = 1;
-            myband = wrapU(wcall > mi ? mi : wcall, is8);
-            const int tmp2 = wrapU(qlen_b + wrapS(P.end_bonus - P.o_del, is8), is8);
-            int md = tmp2 / P.e_del + 1;
-            if (md < 1) md = 1;
-            myband = wrapU(myband > md ? md : myband, is8);
-            wk = wcall < myband ? myband : wcall;
-        }
-        const int qlenE = wrapS(len2, is8);
-        const int tlenE = wrapS(len1, is8);
-        const int mlen = wrapS(imin(wrapU(qlenE + myband, is8), wrapU(tlenE, is8)), is8);
-        const int zdropE = wrapS(P.zdrop, is8);
-        const int bandE = wrapS(myband, is8);
-
-        // ---- row 0 values H_h[k] and F[k] = 0 (:2839-2879)
-        {
-            const int v1 = (h0e > oe_insE) ? wrapS(h0e - oe_insE, is8) : 0;
-            const int top = ncol > 1 ? ncol : 1;
-            for (int k = lane; k <= top; k += 32) {
-                int hv;
-                if (k == 0) hv = h0e;
-                else if (k == 1) hv = v1;
-                else if (k < ncol) hv = imax(v1 - (k - 1) * e_insE, 0);
-                else hv = 0;
-                HF[k] = (uint32_t)hv & 0xffffu;
-            }
-        }
-        __syncwarp();
-
-        // ---- per-pair state (smithWaterman512_16 :3000-3047)
-        int head = 0, tail = qlenE;
-        int maxScore = h0e, x = 0, y = 0, gscore = -1, max_off = 0, max_ie = 0;
-        int beg = 0, end = ncol, nbeg = 0, nend = ncol;
-        const uint32_t full = 0xffffffffu;
-        unsigned long long ncells = 0;
-
-        for (int i = 0; i < nrow; i++) {
-            const int i1 = wrapS(i + 1, is8);
-            beg = nbeg; end = nend;
-            if (beg < i - wk) beg = i - wk;
-            if (end > i + wk + 1) end = i + wk + 1;
-            if (end > ncol) end = ncol;
+        // ---- one row of every active pair (smithWaterman512_16 :3053-3321)
+        bool rowact = active;
+        if (rowact && ps.i >= ps.nrow) { finish(); rowact = false; }
+        const int sh = ps.sh, msk = ps.msk;
+        const int i = ps.i;
+        const int i1 = wrapS(i + 1, sh);
+        int beg = 0, end = 0, h10init = 0;
+        bool changed = false;
+        if (rowact) {
+            beg = ps.nbeg; end = ps.nend;
+            if (beg < i - ps.wk) beg = i - ps.wk;
+            if (end > i + ps.wk + 1) end = i + ps.wk + 1;
+            if (end > ps.ncol) end = ps.ncol;
             // column -1 value: H_v[i+1] (:3065-3067)
-            int h10init = 0;
             if (beg == 0) {
                 const int k = i + 1;
-                if (k == nrow) h10init = 99;  // DUMMY1 past the last row (:2821-2825)
-                else h10init = imax(wrapS(h0e - o_delE - k * e_delE, is8), 0);
+                if (k == ps.nrow) h10init = 99;  // DUMMY1 past the last row (:2821-2825)
+                else h10init = imax(wrapS(ps.h0e - ps.o_delE - k * ps.e_delE, sh), 0);
             }
             // per-pair band (:3080-3089)
-            const int phead = head, ptail = tail;
-            head = imax(head, wrapS(i - bandE, is8));
-            {
-                int t = imin(wrapU(tail, is8), wrapU(i1 + bandE, is8));
-                t = imin(t, wrapU(qlenE, is8));
-                tail = wrapS(t, is8);
-            }
-            // trimming (:3091-3112): zero [beg, min(end, head))
-            if (head != phead || tail != ptail) {
-                const int hi = imin(end, head);
-                for (int l = beg + lane; l < hi; l += 32) HF[l] = 0u;
-                __syncwarp();
-            }
-            // row exit status (:3119-3129); outputs freeze once a pair exits
-            if (i1 > mlen || tail == head || head > tail) break;
-
-            // score lookup for this row's target base: byte q of {thi:tlo} is
-            // S(t, q) + 128 for query code q (0..3 bases, 4 = N); bytes 5..7 are
-            // zero so a selector q | 0x7770 yields the byte zero-extended
-            const int tb = Tt[i];
-            uint32_t tlo, thi;
-            {
-                const uint32_t mis = (uint32_t)(128 - P.b) & 0xffu;
-                const uint32_t mat = (uint32_t)(128 + P.a) & 0xffu;
-                if (tb >= 4) {
-                    tlo = 0x7f7f7f7fu;  // N in the target: -1 against anything
-                } else {
-                    tlo = mis * 0x01010101u;
-                    tlo = (tlo & ~(0xffu << (8 * tb))) | (mat << (8 * tb));
-                }
-                thi = 0x0000007fu;      // N in the query: -1
-            }
-
-            // ---- the row, strip by strip
-            if (end > beg) ncells += (unsigned long long)(end - beg);
-            int carryP = INT_MIN;      // max of P over earlier strips
-            int hprev = h10init;       // H of the column left of the strip
-            uint32_t key = 0;          // (H << 16) | (j + 1), row max, last j wins ties
-            int hq = 0;                // H at column qlen-1
-            int hlast = 0;             // H at column end-1
-            const int sbase = (beg / K) * K;
-            for (int base = sbase; base < end; base += span) {
-                const int j0 = base + lane * K;
-                uint32_t hf[K];
-                int mm[K], ff[K], hh[K];
-                uint32_t qv = 0;
-                const bool anyin = (j0 < end) && (j0 + K - 1 >= beg);
-                if (anyin) {
-                    VecIO<K>::ld(HF + j0, hf);
-                    qv = VecIO<K>::ldq(Q + j0);
-                } else {
-#pragma unroll
-                    for (int k = 0; k < K; k++) hf[k] = 0u;
-                }
-                int summ = INT_MIN;
-#pragma unroll
-                for (int k = 0; k < K; k++) {
-                    const int j = j0 + k;
-                    const int h00 = (int)(hf[k] & 0xffffu);
-                    const int f11 = (int)(hf[k] >> 16);
-                    const uint32_t q = (qv >> (8 * k)) & 0xffu;
-                    const int sbt = (int)__byte_perm(tlo, thi, q | 0x7770u);  // S + 128
-                    const int m = h00 ? h00 + sbt - 128 : 0;
-                    mm[k] = m;
-                    ff[k] = f11;
-                    const int Pk = imax(m - oe_insE, 0) + e_insE * (j - beg);
-                    if (j >= beg && j < end) summ = imax(summ, Pk);
-                }
-                // inclusive max-scan of lane summaries across the warp
-                int incl = summ;
-#pragma unroll
-                for (int d = 1; d < 32; d <<= 1) {
-                    int v = __shfl_up_sync(full, incl, d);
-                    if (lane >= d) incl = imax(incl, v);
-                }
-                int excl = __shfl_up_sync(full, incl, 1);
-                excl = (lane == 0) ? carryP : imax(excl, carryP);
-                carryP = imax(carryP, __shfl_sync(full, incl, 31));
-                int run = excl;
-#pragma unroll
-                for (int k = 0; k < K; k++) {
-                    const int j = j0 + k;
-                    const int E = (j <= beg) ? 0 : run - e_insE * (j - 1 - beg);
-                    const int Pk = imax(mm[k] - oe_insE, 0) + e_insE * (j - beg);
-                    if (j >= beg) run = imax(run, Pk);
-                    hh[k] = imax(imax(mm[k], E), ff[k]);
-                }
-                int hl = __shfl_up_sync(full, hh[K - 1], 1);
-                if (lane == 0) hl = hprev;
-                hprev = __shfl_sync(full, hh[K - 1], 31);
-                uint32_t outv[K];
-#pragma unroll
-                for (int k = 0; k < K; k++) {
-                    const int j = j0 + k;
-                    const bool in = (j >= beg) && (j < end);
-                    const int hleft = (j == beg) ? h10init : ((k == 0) ? hl : hh[k - 1]);
-                    const bool mask = (j < head) || (j > tail);
-                    const int f21 = imax(imax(mm[k] - wrapS(P.o_del + P.e_del, is8), 0),
-                                         ff[k] - e_delE);
-                    const int hst = mask ? 0 : hleft;
-                    const int fst = mask ? 0 : f21;
-                    outv[k] = in ? (((uint32_t)fst << 16) | ((uint32_t)hst & 0xffffu)) : hf[k];
-                    const bool valid = in && !((j + 1) > tail) && !(j < head);
-                    if (valid) {
-                        const uint32_t kk = ((uint32_t)hh[k] << 16) | (uint32_t)(j + 1);
-                        key = kk > key ? kk : key;
-                    }
-                    if (in && j == ncol - 1) hq = hh[k];
-                    if (in && j == end - 1) hlast = hh[k];
-                }
-                if (anyin) VecIO<K>::st(HF + j0, outv);
-            }
-            __syncwarp();
-            key = __reduce_max_sync(full, key);
-            const bool ran = end > beg;
-            hq = __reduce_max_sync(full, (uint32_t)hq);
-            hlast = (int)__reduce_max_sync(full, (uint32_t)hlast);
-            // last column of the row (:3197-3203)
-            {
-                const int jl = ran ? end : beg;
-                const int h10 = ran ? hlast : h10init;
-                const bool m = (head > jl) || (jl > tail);
-                if (lane == 0 && jl <= ncol + 1) HF[jl] = m ? 0u : ((uint32_t)h10 & 0xffffu);
-            }
-            // gscore at the query's last column (:3177-3195)
-            if (ran && (ncol - 1) >= beg && (ncol - 1) < end && !(qlenE > tail)) {
-                max_ie = (gscore > hq) ? max_ie : i1;
-                gscore = imax(gscore, hq);
-            }
-            __syncwarp();
-            const int maxRS1 = (int)(key >> 16);
-            const int y1 = (int)(key & 0xffffu);
-            // a zero row ends the pair (:3206-3211)
-            if (maxRS1 == 0) break;
-            // maximum, its position and max_off (:3213-3226)
-            {
-                const int bmax = maxScore;
-                maxScore = imax(maxScore, maxRS1);
-                if (maxScore > bmax) {
-                    y = y1;
-                    x = i1;
-                    int ind = wrapS(y1 - i1, is8);
-                    if (ind < 0) ind = wrapS(-ind, is8);
-                    max_off = imax(max_off, ind);
-                }
-            }
-            // z-drop (:3229 -> ZSCORE16 :1868-1881, ZSCORE8 :1826-1839)
-            {
-                const int tmpi = wrapS(i1 - x, is8);
-                const int tmpj = wrapS(y1 - y, is8);
-                const int d = (tmpi > tmpj) ? wrapS(tmpi - tmpj, is8) : wrapS(tmpj - tmpi, is8);
-                const int t1 = wrapS(wrapS(maxScore - maxRS1, is8) - d, is8);
-                if (t1 > zdropE) break;
-            }
-            // band narrowing (:3235-3260)
-            {
-                const int f = scan_first_nz(HF, beg, end, lane);
-                if (f > beg) nbeg = f - 1;
-                const int L = scan_last_nz(HF, beg, end, lane);
-                nend = (L + 2 < ncol) ? L + 2 : ncol;
-            }
-            // per-pair head / tail (:3265-3316; the 8-bit kernel scans the
-            // row's own range, :2571-2621)
-            {
-                const int B = is8 ? beg : nbeg;
-                const int E = is8 ? end : nend;
-                if (E > B) {
-                    const int f2 = scan_first_nz(HF, B, E, lane);
-                    if (f2 > B) head = wrapS(f2, is8);
-                }
-                int index = tail;
-                if (E >= B) {
-                    const int L2 = scan_last_nz(HF, B, E, lane);
-                    if (L2 != E) index = L2;
-                }
-                index = wrapS(index + 2, is8);
-                tail = index < qlenE ? index : qlenE;
-            }
+            const int phead = ps.head, ptail = ps.tail;
+            ps.head = imax(ps.head, wrapS(i - ps.bandE, sh));
+            int t = imin(wrapU(ps.tail, msk), wrapU(i1 + ps.bandE, msk));
+            t = imin(t, wrapU(ps.qlenE, msk));
+            ps.tail = wrapS(t, sh);
+            changed = ps.head != phead || ps.tail != ptail;
         }
-        if (lane == 0) {
-            if (A.cells) atomicAdd(A.cells, ncells);
-            pp->score = maxScore;
-            pp->tle = x;
-            pp->qle = y;
-            pp->max_off = max_off;
-            pp->gscore = gscore;
-            pp->gtle = max_ie;
+        // trimming (:3091-3112): zero [beg, min(end, head))
+        if (rowact && changed) {
+            const int hi = imin(end, ps.head);
+            for (int l = beg + gl; l < hi; l += G) { Hh[l] = 0; Fv[l] = 0; }
         }
         __syncwarp();
+        // row exit status (:3119-3129); outputs freeze once a pair exits
+        if (rowact && (i1 > ps.mlen || ps.tail == ps.head || ps.head > ps.tail)) {
+            finish();
+            rowact = false;
+        }
+
+        // score table of this row's target base: byte q of {thi:tlo} is
+        // S(t, q) as a signed byte for query code q (0..3 bases, 4 = N)
+        RowState r;
+        {
+            const int tb = rowact ? Tt[i] : 0;
+            const uint32_t mis = (uint32_t)(-P.b) & 0xffu;
+            const uint32_t mat = (uint32_t)P.a & 0xffu;
+            if (tb >= 4) {
+                r.tlo = 0xffffffffu;  // N in the target: -1 against anything
+            } else {
+                r.tlo = mis * 0x01010101u;
+                r.tlo = (r.tlo & ~(0xffu << (8 * tb))) | (mat << (8 * tb));
+            }
+            r.thi = 0x000000ffu;      // N in the query: -1
+        }
+        r.beg = beg; r.end = end; r.head = ps.head; r.tail = ps.tail;
+        r.carryP = -P.e_ins;          // makes E(beg) = 0
+        r.hprev = h10init;
+        r.h10init = h10init;
+        r.key = 0;
+        r.hlast = 0;
+        const bool ran = rowact && end > beg;
+        if (ran) ps.ncells += (unsigned long long)(end - beg);
+
+        // ---- the row, strip by strip (warp-uniform count and kind)
+        const int sbase = beg & ~(K - 1);
+        const int nstr = ran ? (end - sbase + SPAN - 1) / SPAN : 0;
+        const int smax = (int)__reduce_max_sync(full, (unsigned)nstr);
+        const bool needmask = ran && (ps.head > beg || ps.tail < end);
+        bool lastint = false;
+        for (int s = 0; s < smax; s++) {
+            const int base = sbase + s * SPAN;
+            const bool act = s < nstr;
+            const bool inner = base >= beg && base >= ps.head && base + SPAN <= end &&
+                               base + SPAN <= ps.tail;
+            const int want = (!act || inner) ? STRIP_INTERIOR : (needmask ? STRIP_MASKED : STRIP_EDGE);
+            if (act && s == nstr - 1) lastint = inner;
+            const int mode = (int)__reduce_max_sync(full, (unsigned)want);
+            if (mode == STRIP_INTERIOR) do_strip<G, K, STRIP_INTERIOR>(base, act, gl, r, cc, Hh, Fv, Qs);
+            else if (mode == STRIP_EDGE) do_strip<G, K, STRIP_EDGE>(base, act, gl, r, cc, Hh, Fv, Qs);
+            else do_strip<G, K, STRIP_MASKED>(base, act, gl, r, cc, Hh, Fv, Qs);
+        }
+        __syncwarp();
+        const uint32_t key = group_max<G>(r.key);
+        const int hlast_g = (int)group_max<G>((uint32_t)r.hlast);
+        const int hlast = lastint ? r.hprev : hlast_g;
+        if (rowact) {
+            // last column of the row (:3197-3203)
+            const int jl = ran ? end : beg;
+            const int h10 = ran ? hlast : h10init;
+            const bool m = (ps.head > jl) || (jl > ps.tail);
+            if (gl == 0 && jl <= ps.ncol + 1) {
+                Hh[jl] = m ? 0 : h10;
+                Fv[jl] = 0;
+            }
+            // gscore at the query's last column (:3177-3195); it is in the
+            // band exactly when end == ncol, and then it is column end-1
+            if (ran && end == ps.ncol && !(ps.qlenE > ps.tail)) {
+                ps.max_ie = (ps.gscore > hlast) ? ps.max_ie : i1;
+                ps.gscore = imax(ps.gscore, hlast);
+            }
+        }
+        __syncwarp();
+        if (rowact) {
+            const int maxRS1 = (int)(key >> 16);
+            const int y1 = (int)(key & 0xffffu);
+            if (maxRS1 == 0) {  // a zero row ends the pair (:3206-3211)
+                finish();
+                rowact = false;
+            } else {
+                // maximum, its position and max_off (:3213-3226)
+                const int bmax = ps.maxScore;
+                ps.maxScore = imax(ps.maxScore, maxRS1);
+                if (ps.maxScore > bmax) {
+                    ps.y = y1;
+                    ps.x = i1;
+                    int ind = wrapS(y1 - i1, sh);
+                    if (ind < 0) ind = wrapS(-ind, sh);
+                    ps.max_off = imax(ps.max_off, ind);
+                }
+                // z-drop (:3229 -> ZSCORE16 :1868-1881, ZSCORE8 :1826-1839)
+                const int tmpi = wrapS(i1 - ps.x, sh);
+                const int tmpj = wrapS(y1 - ps.y, sh);
+                const int d = (tmpi > tmpj) ? wrapS(tmpi - tmpj, sh) : wrapS(tmpj - tmpi, sh);
+                const int t1 = wrapS(wrapS(ps.maxScore - maxRS1, sh) - d, sh);
+                if (t1 > ps.zdropE) {
+                    finish();
+                    rowact = false;
+                }
+            }
+        }
+        // band narrowing (:3235-3260)
+        {
+            const int f = scan_first_nz<G>(Hh, Fv, beg, end, rowact, gl, gshift, gbits);
+            const int L = scan_last_nz<G>(Hh, Fv, beg, end, rowact, gl, gshift, gbits);
+            if (rowact) {
+                if (f > beg) ps.nbeg = f - 1;
+                ps.nend = (L + 2 < ps.ncol) ? L + 2 : ps.ncol;
+            }
+        }
+        // per-pair head / tail (:3265-3316; the 8-bit kernel scans the row's
+        // own range, :2571-2621)
+        {
+            const int B = ps.is8 ? beg : ps.nbeg;
+            const int E = ps.is8 ? end : ps.nend;
+            const int f2 = scan_first_nz<G>(Hh, Fv, B, E, rowact && E > B, gl, gshift, gbits);
+            const int L2 = scan_last_nz<G>(Hh, Fv, B, E, rowact && E >= B, gl, gshift, gbits);
+            if (rowact) {
+                if (E > B && f2 > B) ps.head = wrapS(f2, sh);
+                int index = ps.tail;
+                if (E >= B && L2 != E) index = L2;
+                index = wrapS(index + 2, sh);
+                ps.tail = index < ps.qlenE ? index : ps.qlenE;
+                ps.i = i + 1;
+            }
+        }
     }
 }
 

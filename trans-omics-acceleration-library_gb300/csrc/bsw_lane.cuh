@@ -1,0 +1,386 @@
+// Lane-per-pair banded Smith-Waterman for short pairs (sm_103a).
+//
+// Each lane scores its own pair, row by row, exactly as the reference scores
+// one lane of its SIMD group (smithWaterman512_16 / _8, bandedSWA.cpp
+// :2962-3356 / :2263-2661, with the group reduced to that pair -- outputs do
+// not depend on the group).  There are no collectives: lanes are independent
+// and a lane that finishes a pair takes the next one from the work counter.
+// This is the GPU form of the reference's inter-task layout (one pair per SIMD
+// lane), without its shared band: every lane walks its own band.
+//
+// Shared memory per warp, interleaved by lane so that any mix of per-lane
+// columns is bank-conflict free:
+//   HF[col][lane]      H_h (low 16 bits) | F (high 16 bits), the reference's
+//                      scratch rows with their stale values
+//   QS[col/8][lane]    eight query base codes, one nibble each; four nibbles
+//                      are a byte-permute selector that looks up the four
+//                      columns' scores in the row's score table at once
+// The target base of each row is read from global memory (one byte per row).
+//
+// The inner loop over a row's band is split into the columns left of the
+// per-pair head (masked), the clean middle, and the columns at/after the tail,
+// so the middle -- nearly every cell -- runs without predicates.
+#pragma once
+
+#include "bsw_kernel.cuh"
+
+namespace talbsw {
+
+__host__ __device__ __forceinline__ size_t lane_hf_words(int cols_cap) {
+    return (size_t)(cols_cap + 4) * 32;
+}
+__host__ __device__ __forceinline__ size_t lane_qs_words(int cols_cap) {
+    return (size_t)((cols_cap + 7) / 8 + 2) * 32;
+}
+__host__ __device__ __forceinline__ size_t lane_warp_smem_bytes(int cols_cap) {
+    return (lane_hf_words(cols_cap) + lane_qs_words(cols_cap)) * 4;
+}
+
+// Score of query code q (0..4) against the row's table, sign-extended.
+__device__ __forceinline__ int lane_score1(uint32_t tlo, uint32_t thi, uint32_t q) {
+    return prmt_sext(__byte_perm(tlo, thi, q), 0u, 0x8880u);
+}
+
+// One cell of the recurrence (bandedSWA.cpp:1883-1906) given its score sb;
+// returns H(i, j), updates the horizontal gap e, writes the vertical gap f2.
+__device__ __forceinline__ int lane_cell(uint32_t w, int sb, int &e, int &f2, const int oe_ins,
+                                         const int e_ins, const int oe_del, const int e_del) {
+    const int h00 = (int)(w & 0xffffu);
+    const int f = (int)(w >> 16);
+    const int M = __viaddmin_s32(h00, sb, h00 << 12);      // h00 ? h00 + S : <= 0
+    const int H = __vimax3_s32(M, e, f);
+    const int T = __viaddmax_s32_relu(M, -oe_ins, 0);       // max(M - oe_ins, 0)
+    e = __viaddmax_s32(e, -e_ins, T);
+    f2 = __viaddmax_s32_relu(f, -e_del, M - oe_del);
+    return H;
+}
+
+// Per-lane pair state.
+struct LanePair {
+    DevPair *pp;
+    const uint8_t *q, *t;
+    int nrow, ncol, i, initc, tnext;
+    int head, tail, nbeg, nend;
+    int maxScore, x, y, gscore, max_off, max_ie;
+    int h0e, v1, wk, bandE, qlenE, mlen, zdropE, sh, msk;
+    bool is8;
+    unsigned long long ncells;
+};
+
+template <int V>
+__global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
+    TALBSW_DYNAMIC_SMEM(smem_raw);
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    uint32_t *wsm = reinterpret_cast<uint32_t *>(smem_raw) +
+                    (size_t)wib * (lane_hf_words(A.cols_cap) + lane_qs_words(A.cols_cap));
+    uint32_t *HF = wsm + lane;                              // HF[j * 32]
+    uint32_t *QS = wsm + lane_hf_words(A.cols_cap) + lane;  // QS[(j / 8) * 32]
+    const KernelParams P = A.P;
+    const int oe_ins = P.o_ins + P.e_ins, oe_del = P.o_del + P.e_del;
+    const int e_ins = P.e_ins, e_del = P.e_del;
+
+    LanePair s = {};
+    bool active = false;
+    auto fail = [&](int flag, int pidx) {
+        atomicOr(A.err_flags, flag);
+        atomicMin(A.err_index, (long long)pidx);
+    };
+    auto finish = [&]() {
+        if (A.cells) atomicAdd(A.cells, s.ncells);
+        s.pp->score = s.maxScore;
+        s.pp->tle = s.x;
+        s.pp->qle = s.y;
+        s.pp->max_off = s.max_off;
+        s.pp->gscore = s.gscore;
+        s.pp->gtle = s.max_ie;
+        active = false;
+    };
+
+    // One iteration = one row of this lane's pair; a lane that finishes a pair
+    // takes the next one at the top of the next iteration, independently of
+    // the other lanes.
+    for (;;) {
+        if (!active) {
+            const int item = atomicAdd(A.work_counter, 1);
+            if (item >= A.n) break;
+            const int pidx = A.order ? A.order[item] : item;
+            DevPair *pp = A.pairs + pidx;
+            const int len1 = pp->len1, len2 = pp->len2, h0in = pp->h0;
+            const int idr = pp->idr, idq = pp->idq;
+            const int wcall = A.wpair ? A.wpair[pidx] : A.w;
+            bool is8;
+            if (A.bits == 8) is8 = true;
+            else if (A.bits == 16) is8 = false;
+            else is8 = pair_in_range(P, len1, len2, h0in, wcall, true);
+            const bool ok = pair_in_range(P, len1, len2, h0in, wcall, is8) && wcall >= 0 &&
+                            (long long)idr >= A.ref_lo && (long long)idq >= A.qer_lo &&
+                            (long long)idr + len1 <= A.ref_hi && (long long)idq + len2 <= A.qer_hi;
+            if (!ok) { fail(ERR_DOMAIN, pidx); continue; }
+            if (len2 > A.cols_cap) { fail(ERR_CAPACITY, pidx); continue; }
+            // per-pair constants (smithWatermanBatchWrapper16/8 set-up)
+            s.pp = pp;
+            s.q = A.qer + (idq - A.qer_lo);
+            s.t = A.ref + (idr - A.ref_lo);
+            s.nrow = len1; s.ncol = len2; s.i = 0; s.initc = 0; s.ncells = 0;
+            s.is8 = is8;
+            s.sh = is8 ? 24 : 16;
+            s.msk = is8 ? 0xff : 0xffff;
+            const int sh = s.sh, msk = s.msk;
+            s.h0e = wrapS(wrapU(h0in, msk), sh);
+            s.v1 = (s.h0e > oe_ins) ? wrapS(s.h0e - oe_ins, sh) : 0;
+            int maxsc = 0;  // max(0, a, -b, -1) in the element type (:2779-2782)
+            {
+                const int av = wrapS((int8_t)P.a, sh), bv = wrapS((int8_t)(-P.b), sh);
+                if (maxsc < av) maxsc = av;
+                if (maxsc < bv) maxsc = bv;
+                if (maxsc < -1) maxsc = -1;
+            }
+            int myband;  // band clamp (:2882-2904): integer division, then +1
+            {
+                const int qlen_b = wrapU(len2 * maxsc, msk);
+                const int tmp1 = wrapU(qlen_b + wrapS(P.end_bonus - P.o_ins, sh), msk);
+                int mi = tmp1 / P.e_ins + 1;
+                if (mi < 1) mi = 1;
+                myband = wrapU(wcall > mi ? mi : wcall, msk);
+                const int tmp2 = wrapU(qlen_b + wrapS(P.end_bonus - P.o_del, sh), msk);
+                int md = tmp2 / P.e_del + 1;
+                if (md < 1) md = 1;
+                myband = wrapU(myband > md ? md : myband, msk);
+                s.wk = wcall < myband ? myband : wcall;
+            }
+            s.qlenE = wrapS(len2, sh);
+            s.mlen = wrapS(imin(wrapU(s.qlenE + myband, msk), wrapU(wrapS(len1, sh), msk)), sh);
+            s.zdropE = wrapS(P.zdrop, sh);
+            s.bandE = wrapS(myband, sh);
+            s.head = 0; s.tail = s.qlenE;
+            s.maxScore = s.h0e; s.x = 0; s.y = 0; s.gscore = -1; s.max_off = 0; s.max_ie = 0;
+            s.nbeg = 0; s.nend = len2;
+            s.tnext = len1 > 0 ? s.t[0] : 0;
+            active = true;
+        }
+        if (s.i >= s.nrow) { finish(); continue; }
+
+        const int sh = s.sh, msk = s.msk;
+        const int i = s.i, ncol = s.ncol;
+        const int i1 = wrapS(i + 1, sh);
+        const int tb = s.tnext;
+        if (tb > 4) { fail(ERR_BASE, (int)(s.pp - A.pairs)); active = false; continue; }
+        if (i + 1 < s.nrow) s.tnext = s.t[i + 1];
+        // columns up to i + wk + 3 can be touched by this row (band end + 2):
+        // give them their row-0 values and stage their query selectors now
+        {
+            const int lim = imin(imax(ncol, 1), i + s.wk + 3);
+            bool bad = false;
+            for (int k = s.initc; k <= lim; k++) {
+                int hv;
+                if (k == 0) hv = s.h0e;
+                else if (k == 1) hv = s.v1;
+                else if (k < ncol) hv = imax(s.v1 - (k - 1) * e_ins, 0);
+                else hv = 0;
+                HF[k * 32] = (uint32_t)hv;
+                if (!(k & 7) && k < ncol) {
+                    uint32_t wq = 0;
+                    const int m = imin(8, ncol - k);
+                    for (int b = 0; b < m; b++) {
+                        const uint32_t c = s.q[k + b];
+                        bad |= c > 4u;
+                        wq |= (c & 7u) << (4 * b);
+                    }
+                    QS[(k >> 3) * 32] = wq;
+                }
+            }
+            if (lim + 1 > s.initc) s.initc = lim + 1;
+            if (bad) { fail(ERR_BASE, (int)(s.pp - A.pairs)); active = false; continue; }
+        }
+        int beg = s.nbeg, end = s.nend;
+        if (beg < i - s.wk) beg = i - s.wk;
+        if (end > i + s.wk + 1) end = i + s.wk + 1;
+        if (end > ncol) end = ncol;
+        int h10init = 0;  // H_v[i+1] (:3065-3067)
+        if (beg == 0) {
+            const int k = i + 1;
+            h10init = (k == s.nrow) ? 99 : imax(wrapS(s.h0e - P.o_del - k * P.e_del, sh), 0);
+        }
+        // per-pair band (:3080-3089) and trimming (:3091-3112)
+        const int phead = s.head, ptail = s.tail;
+        const int head = imax(s.head, wrapS(i - s.bandE, sh));
+        int tail;
+        {
+            int tt = imin(wrapU(s.tail, msk), wrapU(i1 + s.bandE, msk));
+            tt = imin(tt, wrapU(s.qlenE, msk));
+            tail = wrapS(tt, sh);
+        }
+        s.head = head;
+        s.tail = tail;
+        if (head != phead || tail != ptail) {
+            const int hi = imin(end, head);
+            for (int l = beg; l < hi; l++) HF[l * 32] = 0u;
+        }
+        // row exit status (:3119-3129); outputs freeze once a pair exits
+        if (i1 > s.mlen || tail == head || head > tail) { finish(); continue; }
+
+        // score table of the row's target base: byte q of {thi:tlo} is S(t, q)
+        // as a signed byte (query code q: 0..3 bases, 4 = N)
+        uint32_t tlo;
+        {
+            const uint32_t mis = (uint32_t)(-P.b) & 0xffu;
+            const uint32_t mat = (uint32_t)P.a & 0xffu;
+            if (tb >= 4) {
+                tlo = 0xffffffffu;
+            } else {
+                tlo = mis * 0x01010101u;
+                tlo = (tlo & ~(0xffu << (8 * tb))) | (mat << (8 * tb));
+            }
+        }
+        const uint32_t thi = 0x000000ffu;
+
+        // ---- the band [beg, end): masked left part, clean middle, tail part
+        int e = 0, hprev = h10init;
+        uint32_t key = 0;
+        const int jA = imin(imax(beg, head), end);  // columns j < head: masked
+        const int jB = imax(imin(end, tail), jA);   // columns j >= tail: not in the max
+        if (end > beg) s.ncells += (unsigned long long)(end - beg);
+        for (int j = beg; j < jA; j++) {
+            const uint32_t w = HF[j * 32];
+            const uint32_t q = (QS[(j >> 3) * 32] >> (4 * (j & 7))) & 0xfu;
+            int f2;
+            hprev = lane_cell(w, lane_score1(tlo, thi, q), e, f2, oe_ins, e_ins, oe_del, e_del);
+            HF[j * 32] = 0u;  // masked: H and F stored as zero
+        }
+        {
+            int j = jA;
+            // single columns up to a multiple of 4
+            for (; (j & 3) && j < jB; j++) {
+                const uint32_t w = HF[j * 32];
+                const uint32_t q = (QS[(j >> 3) * 32] >> (4 * (j & 7))) & 0xfu;
+                int f2;
+                const int H = lane_cell(w, lane_score1(tlo, thi, q), e, f2, oe_ins, e_ins, oe_del, e_del);
+                HF[j * 32] = __byte_perm((uint32_t)hprev, (uint32_t)f2, 0x5410u);
+                const uint32_t kk = __byte_perm((uint32_t)(j + 1), (uint32_t)H, 0x5410u);
+                key = kk > key ? kk : key;
+                hprev = H;
+            }
+            // groups of four columns: one table lookup for four scores, the
+            // next group's row words loaded before this group is computed
+            if (j + 3 < jB) {
+                uint32_t w0 = HF[j * 32], w1 = HF[(j + 1) * 32], w2 = HF[(j + 2) * 32],
+                         w3 = HF[(j + 3) * 32];
+                uint32_t qw = QS[(j >> 3) * 32] >> (4 * (j & 4));
+                for (;;) {
+                    const int jn = j + 4;
+                    const bool more = jn + 3 < jB;
+                    uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0, nq = 0;
+                    if (more) {
+                        n0 = HF[jn * 32]; n1 = HF[(jn + 1) * 32];
+                        n2 = HF[(jn + 2) * 32]; n3 = HF[(jn + 3) * 32];
+                        nq = QS[(jn >> 3) * 32] >> (4 * (jn & 4));
+                    }
+                    const uint32_t r4 = __byte_perm(tlo, thi, qw);   // four scores, one per byte
+                    int f20, f21, f22, f23;
+                    const int H0 = lane_cell(w0, prmt_sext(r4, 0u, 0x8880u), e, f20, oe_ins, e_ins, oe_del, e_del);
+                    const int H1 = lane_cell(w1, prmt_sext(r4, 0u, 0x9991u), e, f21, oe_ins, e_ins, oe_del, e_del);
+                    const int H2 = lane_cell(w2, prmt_sext(r4, 0u, 0xaaa2u), e, f22, oe_ins, e_ins, oe_del, e_del);
+                    const int H3 = lane_cell(w3, prmt_sext(r4, 0u, 0xbbb3u), e, f23, oe_ins, e_ins, oe_del, e_del);
+                    HF[j * 32] = __byte_perm((uint32_t)hprev, (uint32_t)f20, 0x5410u);
+                    HF[(j + 1) * 32] = __byte_perm((uint32_t)H0, (uint32_t)f21, 0x5410u);
+                    HF[(j + 2) * 32] = __byte_perm((uint32_t)H1, (uint32_t)f22, 0x5410u);
+                    HF[(j + 3) * 32] = __byte_perm((uint32_t)H2, (uint32_t)f23, 0x5410u);
+                    const uint32_t k0 = __byte_perm((uint32_t)(j + 1), (uint32_t)H0, 0x5410u);
+                    const uint32_t k1 = __byte_perm((uint32_t)(j + 2), (uint32_t)H1, 0x5410u);
+                    const uint32_t k2 = __byte_perm((uint32_t)(j + 3), (uint32_t)H2, 0x5410u);
+                    const uint32_t k3 = __byte_perm((uint32_t)(j + 4), (uint32_t)H3, 0x5410u);
+                    const uint32_t ka = k0 > k1 ? k0 : k1;
+                    const uint32_t kb = k2 > k3 ? k2 : k3;
+                    const uint32_t kc = ka > kb ? ka : kb;
+                    key = kc > key ? kc : key;
+                    hprev = H3;
+                    j = jn;
+                    if (!more) break;
+                    w0 = n0; w1 = n1; w2 = n2; w3 = n3; qw = nq;
+                }
+            }
+            for (; j < jB; j++) {
+                const uint32_t w = HF[j * 32];
+                const uint32_t q = (QS[(j >> 3) * 32] >> (4 * (j & 7))) & 0xfu;
+                int f2;
+                const int H = lane_cell(w, lane_score1(tlo, thi, q), e, f2, oe_ins, e_ins, oe_del, e_del);
+                HF[j * 32] = __byte_perm((uint32_t)hprev, (uint32_t)f2, 0x5410u);
+                const uint32_t kk = __byte_perm((uint32_t)(j + 1), (uint32_t)H, 0x5410u);
+                key = kk > key ? kk : key;
+                hprev = H;
+            }
+        }
+        for (int j = jB; j < end; j++) {
+            const uint32_t w = HF[j * 32];
+            const uint32_t q = (QS[(j >> 3) * 32] >> (4 * (j & 7))) & 0xfu;
+            int f2;
+            const int H = lane_cell(w, lane_score1(tlo, thi, q), e, f2, oe_ins, e_ins, oe_del, e_del);
+            // j >= tail: not in the row maximum; j > tail: H and F stored as zero
+            HF[j * 32] = (j > tail) ? 0u : __byte_perm((uint32_t)hprev, (uint32_t)f2, 0x5410u);
+            hprev = H;
+        }
+        // last column of the row (:3197-3203)
+        const bool ran = end > beg;
+        {
+            const int jl = ran ? end : beg;
+            const bool m = (head > jl) || (jl > tail);
+            if (jl <= ncol + 1) HF[jl * 32] = m ? 0u : ((uint32_t)hprev & 0xffffu);
+        }
+        // gscore at the query's last column (:3177-3195): in the band exactly
+        // when end == ncol, and then it is column end-1
+        if (ran && end == ncol && !(s.qlenE > tail)) {
+            s.max_ie = (s.gscore > hprev) ? s.max_ie : i1;
+            s.gscore = imax(s.gscore, hprev);
+        }
+        const int maxRS1 = (int)(key >> 16);
+        const int y1 = (int)(key & 0xffffu);
+        if (maxRS1 == 0) { finish(); continue; }  // a zero row ends the pair (:3206-3211)
+        {   // maximum, its position and max_off (:3213-3226)
+            const int bmax = s.maxScore;
+            s.maxScore = imax(s.maxScore, maxRS1);
+            if (s.maxScore > bmax) {
+                s.y = y1;
+                s.x = i1;
+                int ind = wrapS(y1 - i1, sh);
+                if (ind < 0) ind = wrapS(-ind, sh);
+                s.max_off = imax(s.max_off, ind);
+            }
+        }
+        {   // z-drop (:3229 -> ZSCORE16 :1868-1881, ZSCORE8 :1826-1839)
+            const int tmpi = wrapS(i1 - s.x, sh);
+            const int tmpj = wrapS(y1 - s.y, sh);
+            const int d = (tmpi > tmpj) ? wrapS(tmpi - tmpj, sh) : wrapS(tmpj - tmpi, sh);
+            const int t1 = wrapS(wrapS(s.maxScore - maxRS1, sh) - d, sh);
+            if (t1 > s.zdropE) { finish(); continue; }
+        }
+        {   // band narrowing (:3235-3260)
+            int l = beg;
+            while (l < end && HF[l * 32] == 0u) l++;
+            if (l > beg) s.nbeg = l - 1;
+            l = end;
+            while (l >= beg && HF[l * 32] == 0u) l--;
+            s.nend = (l + 2 < ncol) ? l + 2 : ncol;
+        }
+        {   // per-pair head / tail (:3265-3316; 8-bit: the row's own range :2571-2621)
+            const int B = s.is8 ? beg : s.nbeg;
+            const int E = s.is8 ? end : s.nend;
+            if (E > B) {
+                int l = B;
+                while (l < E && HF[l * 32] == 0u) l++;
+                if (l > B) s.head = wrapS(l, sh);
+            }
+            int index = s.tail;
+            if (E >= B) {
+                int l = E;
+                while (l >= B && HF[l * 32] == 0u) l--;
+                if (l != E) index = l;
+            }
+            index = wrapS(index + 2, sh);
+            s.tail = index < s.qlenE ? index : s.qlenE;
+        }
+        s.i = i + 1;
+    }
+}
+
+}  // namespace talbsw

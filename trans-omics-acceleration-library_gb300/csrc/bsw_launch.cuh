@@ -1,0 +1,110 @@
+// Launch configuration of the scoring kernel: lanes per pair (G), columns per
+// lane (K), warps per block, grid size.  Shared by the C ABI entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdlib.h>
+
+#include <algorithm>
+
+#include "bsw_kernel.cuh"
+#include "bsw_lane.cuh"
+
+namespace talbsw {
+
+struct KConfig {
+    int G, K;
+};
+
+// Short queries: one lane per pair (G = 1, bsw_lane_kernel), the rows of 32
+// pairs interleaved in a warp's shared memory.  Longer queries: G lanes per
+// pair (bsw_kernel), narrow bands with few lanes (more pairs share each
+// warp-instruction of per-row bookkeeping), wide bands with more lanes so a
+// row is not a long serial walk.  TAL_BSW_G / TAL_BSW_K override (tuning).
+constexpr int kLaneMaxCols = 384;
+
+inline KConfig choose_config(int w, int cols_cap) {
+    long long bw = std::min<long long>(2LL * std::max(w, 0) + 1, (long long)cols_cap);
+    KConfig c;
+    c.K = 4;
+    if (cols_cap <= kLaneMaxCols) c.G = 1;
+    else if (bw <= 64) c.G = 4;
+    else if (bw <= 256) c.G = 8;
+    else if (bw <= 640) c.G = 16;
+    else c.G = 32;
+    if (const char *e = getenv("TAL_BSW_G")) {
+        int g = atoi(e);
+        if (g == 1 || g == 4 || g == 8 || g == 16 || g == 32) c.G = g;
+    }
+    if (const char *e = getenv("TAL_BSW_K")) {
+        int k = atoi(e);
+        if (k == 2 || k == 4) c.K = k;
+    }
+    return c;
+}
+
+template <int G, int K>
+inline cudaError_t launch_gk(const LaunchArgs &A, int num_sms, size_t smem_optin, cudaStream_t s) {
+    auto kern = bsw_kernel<G, K>;
+    const size_t wbytes = warp_smem_bytes(A.cols_cap, A.rows_cap, G);
+    int wpb = 4;
+    while (wpb > 1 && (size_t)wpb * wbytes * 2 > smem_optin) wpb >>= 1;
+    const size_t smem = (size_t)wpb * wbytes;
+    if (smem > smem_optin) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int bps = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, smem);
+    if (e != cudaSuccess) return e;
+    if (bps < 1) return cudaErrorInvalidConfiguration;
+    long long blocks = (long long)bps * num_sms;
+    const long long pairs_per_block = (long long)wpb * (32 / G);
+    const long long need = ((long long)A.n + pairs_per_block - 1) / pairs_per_block;
+    if (blocks > need) blocks = std::max<long long>(need, 1);
+    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(A);
+    return cudaGetLastError();
+}
+
+inline cudaError_t launch_lane(const LaunchArgs &A, int num_sms, size_t smem_optin, cudaStream_t s) {
+    auto kern = bsw_lane_kernel<0>;
+    const size_t wbytes = lane_warp_smem_bytes(A.cols_cap);
+    int wpb = 4;
+    while (wpb > 1 && (size_t)wpb * wbytes > 48 * 1024) wpb >>= 1;
+    const size_t smem = (size_t)wpb * wbytes;
+    if (smem > smem_optin) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int bps = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, smem);
+    if (e != cudaSuccess) return e;
+    if (bps < 1) return cudaErrorInvalidConfiguration;
+    long long blocks = (long long)bps * num_sms;
+    const long long need = ((long long)A.n + 32LL * wpb - 1) / (32LL * wpb);
+    if (blocks > need) blocks = std::max<long long>(need, 1);
+    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(A);
+    return cudaGetLastError();
+}
+
+// Shared memory one warp of the chosen configuration needs.
+inline size_t config_smem(const KConfig &c, int cols_cap, int rows_cap) {
+    if (c.G == 1) return lane_warp_smem_bytes(cols_cap);
+    return warp_smem_bytes(cols_cap, rows_cap, c.G);
+}
+
+inline cudaError_t launch_config(const LaunchArgs &A, const KConfig &c, int num_sms,
+                                 size_t smem_optin, cudaStream_t s) {
+    if (c.G == 1) return launch_lane(A, num_sms, smem_optin, s);
+    switch (c.G * 10 + c.K) {
+        case 44: return launch_gk<4, 4>(A, num_sms, smem_optin, s);
+        case 42: return launch_gk<4, 2>(A, num_sms, smem_optin, s);
+        case 84: return launch_gk<8, 4>(A, num_sms, smem_optin, s);
+        case 82: return launch_gk<8, 2>(A, num_sms, smem_optin, s);
+        case 164: return launch_gk<16, 4>(A, num_sms, smem_optin, s);
+        case 162: return launch_gk<16, 2>(A, num_sms, smem_optin, s);
+        case 324: return launch_gk<32, 4>(A, num_sms, smem_optin, s);
+        case 322: return launch_gk<32, 2>(A, num_sms, smem_optin, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace talbsw

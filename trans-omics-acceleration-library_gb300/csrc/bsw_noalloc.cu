@@ -23,7 +23,7 @@
 #include <mutex>
 
 #include "../../include/tal_bsw.h"
-#include "bsw_kernel.cuh"
+#include "bsw_launch.cuh"
 
 namespace {
 
@@ -93,22 +93,6 @@ int setup_device(int dev) {
     return TAL_OK;
 }
 
-template <int K>
-cudaError_t launch(const talbsw::LaunchArgs &A, int dev, int wpb, size_t smem, cudaStream_t s) {
-    auto kern = talbsw::bsw_warp_kernel<K>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int bps = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, smem);
-    if (e != cudaSuccess) return e;
-    if (bps < 1) return cudaErrorInvalidConfiguration;
-    long long blocks = (long long)bps * g_num_sms[dev];
-    long long need = ((long long)A.n + wpb - 1) / wpb;
-    if (blocks > need) blocks = std::max<long long>(need, 1);
-    kern<<<(unsigned)blocks, 32 * wpb, smem, s>>>(A);
-    return cudaGetLastError();
-}
-
 }  // namespace
 
 extern "C" int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_seq_pair *d_pairs,
@@ -162,16 +146,10 @@ extern "C" int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_s
     A.err_index = &c->bad_index;
     A.cells = &c->cells;
     A.P = {p.o_del, p.e_del, p.o_ins, p.e_ins, p.zdrop, p.end_bonus, p.w_match, p.w_mismatch};
-    long long band = std::min<long long>(2LL * std::max(w, 0) + 1, (long long)A.cols_cap);
-    const int K = band <= 40 ? 1 : band <= 100 ? 2 : 4;
-    const size_t wbytes = talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, K);
-    int wpb = 4;
-    while (wpb > 1 && (size_t)wpb * wbytes * 2 > g_smem_optin[dev]) wpb >>= 1;
-    const size_t smem = (size_t)wpb * wbytes;
-    if (smem > g_smem_optin[dev]) return TAL_EDOMAIN;  // a pair too long for shared memory
-    if (K == 1) e = launch<1>(A, dev, wpb, smem, s);
-    else if (K == 2) e = launch<2>(A, dev, wpb, smem, s);
-    else e = launch<4>(A, dev, wpb, smem, s);
+    const talbsw::KConfig cfg = talbsw::choose_config(w, A.cols_cap);
+    if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap) > g_smem_optin[dev])
+        return TAL_EDOMAIN;  // a pair too long for the shared-memory rows
+    e = talbsw::launch_config(A, cfg, g_num_sms[dev], g_smem_optin[dev], s);
     if (e != cudaSuccess) return TAL_ECUDA;
     int flags = 0;
     e = cudaMemcpyAsync(&flags, &c->flags, sizeof(flags), cudaMemcpyDeviceToHost, s);
