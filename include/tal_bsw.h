@@ -96,6 +96,35 @@ int tal_bsw_scores_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t
                           size_t ref_bytes, const uint8_t *d_qer, size_t qer_bytes,
                           int32_t numPairs, int32_t w, const int32_t *d_w, int bits);
 
+/* Batched form, no counterpart in the reference (its callers issue one
+ * getScores call per batch): scores a large batch of mixed pairs -- uneven
+ * lengths, per-pair bands (d_w / wpair, optional), 8/16-bit routing with
+ * bits = TAL_BSW_AUTO -- as one CUDA graph: a device-side sort of the pairs
+ * into length bins (by query length, then target length) followed by one
+ * persistent, work-stealing launch per bin, each with the kernel and tile an
+ * autotuner picked for that bin on the handle's first batched call.  Outputs
+ * are the same as tal_bsw_scores on the same pairs.  The graph is captured on
+ * the first call with a given set of buffers and replayed after that.
+ * Device-resident variant; synchronous (returns the status). */
+int tal_bsw_scores_batched_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t *d_ref,
+                                  size_t ref_bytes, const uint8_t *d_qer, size_t qer_bytes,
+                                  int32_t numPairs, int32_t w, const int32_t *d_w, int bits);
+
+/* The batched form on host buffers (pairs updated in place); wpair: an
+ * optional band per pair. */
+int tal_bsw_scores_batched(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufRef,
+                           const uint8_t *seqBufQer, int32_t numPairs, int32_t w,
+                           const int32_t *wpair, int bits);
+
+/* Forgets the autotuner's choices and the captured graphs (the next batched
+ * call tunes again). */
+int tal_bsw_autotune_reset(tal_bsw_handle h);
+
+/* The configuration of length bin `bin` (0..20): lanes per pair (1 = the
+ * lane-per-pair kernel), columns per lane, and the bin's largest query length. */
+int tal_bsw_bin_config(tal_bsw_handle h, int bin, int *lanes_per_pair, int *cols_per_lane,
+                       int *max_len2);
+
 /* Waits for the handle's stream; returns the first error any launch on it
  * reported since the last sync. */
 int tal_bsw_sync(tal_bsw_handle h);

@@ -11,52 +11,12 @@
 #include <mutex>
 #include <string>
 
-#include "../../include/tal_bsw.h"
-#include "bsw_launch.cuh"
+#include "bsw_ctx.h"
 
 static_assert(sizeof(tal_seq_pair) == 56, "SeqPair is 14 x int32 (bandedSWA.h:90-99)");
 static_assert(sizeof(talbsw::DevPair) == 56, "device SeqPair view");
 
-namespace {
-
-struct DevBuf {
-    void *p = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
-        if (bytes <= cap) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t want = std::max(bytes, cap + cap / 2);
-        want = (want + 255) & ~(size_t)255;
-        cudaError_t e = cudaMalloc(&p, want);
-        if (e == cudaSuccess) cap = want;
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
-
-}  // namespace
-
-struct tal_bsw_ctx {
-    tal_bsw_params prm;
-    talbsw::KernelParams kp;
-    int device = 0;
-    int num_sms = 0;
-    size_t smem_optin = 0;
-    cudaStream_t stream = nullptr;
-    DevBuf pairs, ref, qer, ctrl, wpair, caps;
-    std::mutex mu;
-    std::string last_error;
-    int64_t last_bad = -1;
-    uint64_t launches = 0;
-    uint64_t last_cells = 0;
-    int pending_status = TAL_OK;
-};
+using talbsw::DevBuf;
 
 namespace {
 
@@ -85,7 +45,8 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
     A.err_index = &c->bad_index;
     A.cells = &c->cells;
     A.P = h->kp;
-    const talbsw::KConfig cfg = talbsw::choose_config(w_for_k, A.cols_cap);
+    const talbsw::KConfig cfg =
+        talbsw::fit_config(talbsw::choose_config(w_for_k, A.cols_cap), A.cols_cap, h->smem_optin);
     if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap) > h->smem_optin)
         return fail(h, TAL_EDOMAIN, "pair too long for the shared-memory row buffers");
     Ctrl init = {0, 0, (long long)INT64_MAX, 0ull};
@@ -169,6 +130,13 @@ int tal_bsw_destroy(tal_bsw_handle h) {
         h->ctrl.release();
         h->wpair.release();
         h->caps.release();
+        h->bcounts.release();
+        h->border.release();
+        h->bseg.release();
+        h->bctrl.release();
+        h->btune_seg.release();
+        for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second.exec);
+        h->graphs.clear();
         cudaStreamDestroy(h->stream);
     }
     delete h;

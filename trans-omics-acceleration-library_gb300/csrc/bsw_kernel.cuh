@@ -67,6 +67,7 @@ struct LaunchArgs {
     const uint8_t *qer;
     long long ref_lo, ref_hi, qer_lo, qer_hi;
     const int32_t *order;    // optional permutation (batched form)
+    const int32_t *seg;      // optional {offset, count} into order (overrides n)
     const int32_t *wpair;    // optional per-pair band
     int32_t n;
     int32_t w;
@@ -152,8 +153,8 @@ struct VecIO<4> {
 constexpr int KPAD = 4;  // widest strip's columns per lane: row padding
 
 // Shared-memory footprint of one pair's rows, in bytes (16-byte aligned parts):
-// H_h and F (int32 each), the query as 16-bit byte-permute selectors, the
-// target as base codes.
+// H_h and F (int32 each) and the query as 16-bit byte-permute selectors.  The
+// target is read from global memory, one base per row.
 __host__ __device__ __forceinline__ size_t smem_hh_bytes(int cols_cap) {
     return ((size_t)(cols_cap + 2 + KPAD) * 4 + 15) & ~(size_t)15;
 }
@@ -161,8 +162,8 @@ __host__ __device__ __forceinline__ size_t smem_q_bytes(int cols_cap) {
     return ((size_t)(cols_cap + KPAD + 8) * 2 + 15) & ~(size_t)15;
 }
 __host__ __device__ __forceinline__ size_t pair_smem_bytes(int cols_cap, int rows_cap) {
-    size_t t = ((size_t)(rows_cap + 16) + 15) & ~(size_t)15;
-    return 2 * smem_hh_bytes(cols_cap) + smem_q_bytes(cols_cap) + t;
+    (void)rows_cap;
+    return 2 * smem_hh_bytes(cols_cap) + smem_q_bytes(cols_cap);
 }
 // one warp = 32/G pairs
 __host__ __device__ __forceinline__ size_t warp_smem_bytes(int cols_cap, int rows_cap, int G) {
@@ -438,7 +439,8 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
     int *Hh = reinterpret_cast<int *>(pbase);
     int *Fv = reinterpret_cast<int *>(pbase + smem_hh_bytes(A.cols_cap));
     uint16_t *Qs = reinterpret_cast<uint16_t *>(pbase + 2 * smem_hh_bytes(A.cols_cap));
-    uint8_t *Tt = pbase + 2 * smem_hh_bytes(A.cols_cap) + smem_q_bytes(A.cols_cap);
+    const uint8_t *Tg = nullptr;  // this pair's target in global memory
+    int tnext = 0;                // its next row's base, loaded one row ahead
     const KernelParams P = A.P;
 
     CellConsts cc;
@@ -457,6 +459,8 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
     PairState ps;
     ps.pidx = 0; ps.nrow = 0; ps.ncol = 0; ps.i = 0; ps.ncells = 0;
     bool active = false, done = false;
+    const int nwork = A.seg ? A.seg[1] : A.n;
+    const int32_t *order = A.seg ? A.order + A.seg[0] : A.order;
 
     auto finish = [&]() {
         if (gl == 0) {
@@ -479,12 +483,12 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             int item = 0;
             if (need && gl == 0) item = atomicAdd(A.work_counter, 1);
             item = __shfl_sync(full, item, gshift);
-            const bool take = need && item < A.n;
+            const bool take = need && item < nwork;
             if (need && !take) done = true;
             int len1 = 0, len2 = 0, h0in = 0, idr = 0, idq = 0, wcall = 0, pidx = 0;
             bool is8 = false, ok = false;
             if (take) {
-                pidx = A.order ? A.order[item] : item;
+                pidx = order ? order[item] : item;
                 const DevPair *pp = A.pairs + pidx;
                 len1 = pp->len1; len2 = pp->len2; h0in = pp->h0;
                 idr = pp->idr; idq = pp->idq;
@@ -500,7 +504,7 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
                         atomicOr(A.err_flags, ERR_DOMAIN);
                         atomicMin(A.err_index, (long long)pidx);
                     }
-                } else if (len2 > A.cols_cap || len1 > A.rows_cap) {
+                } else if (len2 > A.cols_cap) {
                     ok = false;
                     if (gl == 0) {
                         atomicOr(A.err_flags, ERR_CAPACITY);
@@ -513,9 +517,6 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             bool bad = stage_bases<G, uint16_t, 0x1111u, 0x8880u>(
                 Qs, A.qer, st ? len2 : 0, (size_t)(A.qer_hi - A.qer_lo),
                 st ? (size_t)(idq - A.qer_lo) : 0, gl);
-            bad |= stage_bases<G, uint8_t, 1u, 0u>(
-                Tt, A.ref, st ? len1 : 0, (size_t)(A.ref_hi - A.ref_lo),
-                st ? (size_t)(idr - A.ref_lo) : 0, gl);
             const unsigned bm = __ballot_sync(full, bad) & gbits;
             if (st && bm) {
                 if (gl == 0) {
@@ -529,6 +530,8 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
                 const int sh = is8 ? 24 : 16, msk = is8 ? 0xff : 0xffff;
                 ps.is8 = is8; ps.sh = sh; ps.msk = msk;
                 ps.pidx = pidx; ps.nrow = len1; ps.ncol = len2; ps.i = 0; ps.ncells = 0;
+                Tg = A.ref + (idr - A.ref_lo);
+                tnext = len1 > 0 ? Tg[0] : 0;
                 ps.h0e = wrapS(wrapU(h0in, msk), sh);
                 ps.o_delE = P.o_del;
                 ps.e_delE = P.e_del;
@@ -623,7 +626,16 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
         // S(t, q) as a signed byte for query code q (0..3 bases, 4 = N)
         RowState r;
         {
-            const int tb = rowact ? Tt[i] : 0;
+            const int tb = rowact ? tnext : 0;
+            if (rowact && i + 1 < ps.nrow) tnext = Tg[i + 1];
+            if (rowact && tb > 4) {  // a target base code above 4
+                if (gl == 0) {
+                    atomicOr(A.err_flags, ERR_BASE);
+                    atomicMin(A.err_index, (long long)ps.pidx);
+                }
+                active = false;
+                rowact = false;
+            }
             const uint32_t mis = (uint32_t)(-P.b) & 0xffu;
             const uint32_t mat = (uint32_t)P.a & 0xffu;
             if (tb >= 4) {

@@ -55,6 +55,51 @@ __device__ __forceinline__ int lane_cell(uint32_t w, int sb, int &e, int &f2, co
     return H;
 }
 
+// Four consecutive columns j..j+3 of a row (row words w0..w3 at hp[0],
+// hp[32], hp[64], hp[96]); qw: their four query codes as a selector.  SYM:
+// o_del == o_ins and e_del == e_ins, so the vertical gap reuses max(M - oe, 0).
+template <bool SYM>
+__device__ __forceinline__ void lane_group4(uint32_t *hp, int j, uint32_t w0, uint32_t w1,
+                                            uint32_t w2, uint32_t w3, uint32_t qw, uint32_t tlo,
+                                            uint32_t thi, int &e, int &hprev, uint32_t &key,
+                                            const int oe_ins, const int e_ins, const int oe_del,
+                                            const int e_del) {
+    const uint32_t r4 = __byte_perm(tlo, thi, qw);  // four scores, one per byte
+    const uint32_t w[4] = {w0, w1, w2, w3};
+    int M[4], T[4], f[4], H[4], f2[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int sb = prmt_sext(r4, 0u, 0x8880u + 0x1111u * (uint32_t)k);
+        const int h00 = (int)(w[k] & 0xffffu);
+        f[k] = (int)(w[k] >> 16);
+        M[k] = __viaddmin_s32(h00, sb, h00 << 12);       // h00 ? h00 + S : <= 0
+        T[k] = __viaddmax_s32_relu(M[k], -oe_ins, 0);     // max(M - oe_ins, 0)
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        H[k] = __vimax3_s32(M[k], e, f[k]);
+        e = __viaddmax_s32(e, -e_ins, T[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (SYM) f2[k] = __viaddmax_s32(f[k], -e_del, T[k]);
+        else f2[k] = __viaddmax_s32_relu(f[k], -e_del, M[k] - oe_del);
+    }
+    hp[0] = __byte_perm((uint32_t)hprev, (uint32_t)f2[0], 0x5410u);
+    hp[32] = __byte_perm((uint32_t)H[0], (uint32_t)f2[1], 0x5410u);
+    hp[64] = __byte_perm((uint32_t)H[1], (uint32_t)f2[2], 0x5410u);
+    hp[96] = __byte_perm((uint32_t)H[2], (uint32_t)f2[3], 0x5410u);
+    const uint32_t k0 = __byte_perm((uint32_t)(j + 1), (uint32_t)H[0], 0x5410u);
+    const uint32_t k1 = __byte_perm((uint32_t)(j + 2), (uint32_t)H[1], 0x5410u);
+    const uint32_t k2 = __byte_perm((uint32_t)(j + 3), (uint32_t)H[2], 0x5410u);
+    const uint32_t k3 = __byte_perm((uint32_t)(j + 4), (uint32_t)H[3], 0x5410u);
+    const uint32_t ka = k0 > k1 ? k0 : k1;
+    const uint32_t kb = k2 > k3 ? k2 : k3;
+    const uint32_t kc = ka > kb ? ka : kb;
+    key = kc > key ? kc : key;
+    hprev = H[3];
+}
+
 // Per-lane pair state.
 struct LanePair {
     DevPair *pp;
@@ -67,8 +112,11 @@ struct LanePair {
     unsigned long long ncells;
 };
 
+// V bit 0: plain group loop (else explicit prefetch of the next group);
+// V bit 1: symmetric gap parameters (o_del == o_ins, e_del == e_ins).
 template <int V>
 __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
+    constexpr bool SYM = (V & 2) != 0;
     TALBSW_DYNAMIC_SMEM(smem_raw);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -82,6 +130,8 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
 
     LanePair s = {};
     bool active = false;
+    const int nwork = A.seg ? A.seg[1] : A.n;
+    const int32_t *order = A.seg ? A.order + A.seg[0] : A.order;
     auto fail = [&](int flag, int pidx) {
         atomicOr(A.err_flags, flag);
         atomicMin(A.err_index, (long long)pidx);
@@ -103,8 +153,8 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
     for (;;) {
         if (!active) {
             const int item = atomicAdd(A.work_counter, 1);
-            if (item >= A.n) break;
-            const int pidx = A.order ? A.order[item] : item;
+            if (item >= nwork) break;
+            const int pidx = order ? order[item] : item;
             DevPair *pp = A.pairs + pidx;
             const int len1 = pp->len1, len2 = pp->len2, h0in = pp->h0;
             const int idr = pp->idr, idq = pp->idq;
@@ -261,43 +311,38 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                 key = kk > key ? kk : key;
                 hprev = H;
             }
-            // groups of four columns: one table lookup for four scores, the
-            // next group's row words loaded before this group is computed
-            if (j + 3 < jB) {
-                uint32_t w0 = HF[j * 32], w1 = HF[(j + 1) * 32], w2 = HF[(j + 2) * 32],
-                         w3 = HF[(j + 3) * 32];
-                uint32_t qw = QS[(j >> 3) * 32] >> (4 * (j & 4));
-                for (;;) {
-                    const int jn = j + 4;
-                    const bool more = jn + 3 < jB;
-                    uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0, nq = 0;
-                    if (more) {
-                        n0 = HF[jn * 32]; n1 = HF[(jn + 1) * 32];
-                        n2 = HF[(jn + 2) * 32]; n3 = HF[(jn + 3) * 32];
-                        nq = QS[(jn >> 3) * 32] >> (4 * (jn & 4));
+            // groups of four columns: one table lookup for four scores
+            if constexpr ((V & 1) == 0) {
+                // next group's row words loaded before this group is computed
+                if (j + 3 < jB) {
+                    uint32_t w0 = HF[j * 32], w1 = HF[(j + 1) * 32], w2 = HF[(j + 2) * 32],
+                             w3 = HF[(j + 3) * 32];
+                    uint32_t qw = QS[(j >> 3) * 32] >> (4 * (j & 4));
+                    for (;;) {
+                        const int jn = j + 4;
+                        const bool more = jn + 3 < jB;
+                        uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0, nq = 0;
+                        if (more) {
+                            n0 = HF[jn * 32]; n1 = HF[(jn + 1) * 32];
+                            n2 = HF[(jn + 2) * 32]; n3 = HF[(jn + 3) * 32];
+                            nq = QS[(jn >> 3) * 32] >> (4 * (jn & 4));
+                        }
+                        lane_group4<SYM>(HF + j * 32, j, w0, w1, w2, w3, qw, tlo, thi, e, hprev, key,
+                                         oe_ins, e_ins, oe_del, e_del);
+                        j = jn;
+                        if (!more) break;
+                        w0 = n0; w1 = n1; w2 = n2; w3 = n3; qw = nq;
                     }
-                    const uint32_t r4 = __byte_perm(tlo, thi, qw);   // four scores, one per byte
-                    int f20, f21, f22, f23;
-                    const int H0 = lane_cell(w0, prmt_sext(r4, 0u, 0x8880u), e, f20, oe_ins, e_ins, oe_del, e_del);
-                    const int H1 = lane_cell(w1, prmt_sext(r4, 0u, 0x9991u), e, f21, oe_ins, e_ins, oe_del, e_del);
-                    const int H2 = lane_cell(w2, prmt_sext(r4, 0u, 0xaaa2u), e, f22, oe_ins, e_ins, oe_del, e_del);
-                    const int H3 = lane_cell(w3, prmt_sext(r4, 0u, 0xbbb3u), e, f23, oe_ins, e_ins, oe_del, e_del);
-                    HF[j * 32] = __byte_perm((uint32_t)hprev, (uint32_t)f20, 0x5410u);
-                    HF[(j + 1) * 32] = __byte_perm((uint32_t)H0, (uint32_t)f21, 0x5410u);
-                    HF[(j + 2) * 32] = __byte_perm((uint32_t)H1, (uint32_t)f22, 0x5410u);
-                    HF[(j + 3) * 32] = __byte_perm((uint32_t)H2, (uint32_t)f23, 0x5410u);
-                    const uint32_t k0 = __byte_perm((uint32_t)(j + 1), (uint32_t)H0, 0x5410u);
-                    const uint32_t k1 = __byte_perm((uint32_t)(j + 2), (uint32_t)H1, 0x5410u);
-                    const uint32_t k2 = __byte_perm((uint32_t)(j + 3), (uint32_t)H2, 0x5410u);
-                    const uint32_t k3 = __byte_perm((uint32_t)(j + 4), (uint32_t)H3, 0x5410u);
-                    const uint32_t ka = k0 > k1 ? k0 : k1;
-                    const uint32_t kb = k2 > k3 ? k2 : k3;
-                    const uint32_t kc = ka > kb ? ka : kb;
-                    key = kc > key ? kc : key;
-                    hprev = H3;
-                    j = jn;
-                    if (!more) break;
-                    w0 = n0; w1 = n1; w2 = n2; w3 = n3; qw = nq;
+                }
+            } else {
+                // plain loop over groups; two groups per iteration so that
+                // the second group's loads can be issued early
+                uint32_t *hp = HF + j * 32;
+#pragma unroll 2
+                for (; j + 3 < jB; j += 4, hp += 128) {
+                    const uint32_t qw = QS[(j >> 3) * 32] >> (4 * (j & 4));
+                    lane_group4<SYM>(hp, j, hp[0], hp[32], hp[64], hp[96], qw, tlo, thi, e, hprev,
+                                     key, oe_ins, e_ins, oe_del, e_del);
                 }
             }
             for (; j < jB; j++) {

@@ -66,7 +66,12 @@ inline cudaError_t launch_gk(const LaunchArgs &A, int num_sms, size_t smem_optin
 }
 
 inline cudaError_t launch_lane(const LaunchArgs &A, int num_sms, size_t smem_optin, cudaStream_t s) {
-    auto kern = bsw_lane_kernel<0>;
+    const bool sym = A.P.o_del == A.P.o_ins && A.P.e_del == A.P.e_ins;
+    int v = sym ? 3 : 1;
+    if (const char *ev = getenv("TAL_BSW_LV")) v = atoi(ev) & 3;
+    if (!sym) v &= 1;
+    auto kern = v == 0 ? bsw_lane_kernel<0> : v == 1 ? bsw_lane_kernel<1>
+              : v == 2 ? bsw_lane_kernel<2> : bsw_lane_kernel<3>;
     const size_t wbytes = lane_warp_smem_bytes(A.cols_cap);
     int wpb = 4;
     while (wpb > 1 && (size_t)wpb * wbytes > 48 * 1024) wpb >>= 1;
@@ -89,6 +94,13 @@ inline cudaError_t launch_lane(const LaunchArgs &A, int num_sms, size_t smem_opt
 inline size_t config_smem(const KConfig &c, int cols_cap, int rows_cap) {
     if (c.G == 1) return lane_warp_smem_bytes(cols_cap);
     return warp_smem_bytes(cols_cap, rows_cap, c.G);
+}
+
+// Widens the lanes per pair (fewer pairs per warp, less shared memory per
+// warp) until one warp's rows fit a block.
+inline KConfig fit_config(KConfig c, int cols_cap, size_t smem_optin) {
+    while (c.G < 32 && config_smem(c, cols_cap, 1) > smem_optin) c.G = c.G == 1 ? 4 : c.G * 2;
+    return c;
 }
 
 inline cudaError_t launch_config(const LaunchArgs &A, const KConfig &c, int num_sms,

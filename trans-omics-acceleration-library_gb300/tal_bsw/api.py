@@ -53,6 +53,16 @@ _SIGS = {
     "tal_bsw_last_bad_pair": (ctypes.c_int64, [ctypes.c_void_p]),
     "tal_bsw_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
     "tal_bsw_last_cells": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "tal_bsw_scores_batched_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                                     ctypes.c_int]),
+    "tal_bsw_scores_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                              ctypes.c_void_p, ctypes.c_int]),
+    "tal_bsw_autotune_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "tal_bsw_bin_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "tal_bsw_probe_int_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_double)]),
 }
@@ -129,6 +139,40 @@ class BandedPairWiseSW:
         self._check(rc)
         if sync:
             self.sync()
+
+    # -- batched form --------------------------------------------------------------
+    def scores_batched(self, pairArray, seqBufRef, seqBufQer, numPairs: int, w: int = 100,
+                       wpair: Optional[np.ndarray] = None, bits: int = AUTO) -> None:
+        """Length-binned, autotuned, graph-captured scoring of a mixed batch on
+        host buffers (pairs updated in place); wpair: optional band per pair."""
+        pa = _as_pairs(pairArray)
+        n = int(numPairs)
+        if n < 0 or n > pa.shape[0]:
+            raise ValueError("numPairs out of range for pairArray")
+        wp = None
+        if wpair is not None:
+            wpair = np.ascontiguousarray(wpair, np.int32)
+            if wpair.shape[0] < n:
+                raise ValueError("wpair shorter than numPairs")
+            wp = wpair.ctypes.data
+        self._check(self._lib.tal_bsw_scores_batched(self._h, pa.ctypes.data, _buf_ptr(seqBufRef),
+                                                     _buf_ptr(seqBufQer), n, int(w), wp, int(bits)))
+
+    def scores_batched_device(self, d_pairs: int, d_ref: int, ref_bytes: int, d_qer: int,
+                              qer_bytes: int, numPairs: int, w: int, bits: int = AUTO,
+                              d_w: Optional[int] = None) -> None:
+        self._check(self._lib.tal_bsw_scores_batched_device(self._h, d_pairs, d_ref, ref_bytes, d_qer,
+                                                            qer_bytes, int(numPairs), int(w), d_w,
+                                                            int(bits)))
+
+    def autotune_reset(self) -> None:
+        self._check(self._lib.tal_bsw_autotune_reset(self._h))
+
+    def bin_config(self, b: int):
+        g, k, m = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self._lib.tal_bsw_bin_config(self._h, int(b), ctypes.byref(g), ctypes.byref(k),
+                                                 ctypes.byref(m)))
+        return g.value, k.value, m.value
 
     def sync(self) -> None:
         self._check(self._lib.tal_bsw_sync(self._h))
