@@ -55,6 +55,10 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling)")
     ap.add_argument("--pairs", type=int, default=None,
                     help="score only the first N pairs of the workload (profiling a small case)")
+    ap.add_argument("--no-mixed", action="store_true",
+                    help="skip the mixed-length plain-vs-batched comparison")
+    ap.add_argument("--mixed-pairs", type=int, default=None,
+                    help="pairs of the mixed-length workload (default: all 10,000,000)")
     return ap.parse_args()
 
 
@@ -329,6 +333,26 @@ def run_ours(args):
     dev_out = dp.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE)
     agree = bool((tal_bsw.outputs(dev_out) == tal_bsw.outputs(hpairs)).all())
 
+    # ---- batched form on the same pairs (device-resident)
+    def step_batched():
+        bsw.scores_batched_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                                  n, wl.w, bits)
+    for _ in range(max(args.warmup, 3)):
+        step_batched()
+    dist.barrier()
+    torch.cuda.synchronize()
+    b0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_batched()
+    torch.cuda.synchronize()
+    t_batched = dist.max((time.perf_counter() - b0) / args.steps)
+    batched = {"value": round(total_cells / t_batched / 1e9, 3), "unit": UNIT,
+               "pairs_per_s": round(total_pairs / t_batched, 1),
+               "ms_per_step": round(t_batched * 1e3, 3),
+               "bins": [list(bsw.bin_config(k)[:2]) for k in range(21)],
+               "note": "device-resident batched call (sort into length bins + per-bin "
+                       "persistent launches, one CUDA graph); wall time per synchronous call"}
+
     # ---- rooflines
     hbm_peak, peak_src = measured_peaks()
     alg_bytes = lens + 56 * n + 24 * n          # bases read, SeqPair read, outputs written
@@ -363,7 +387,10 @@ def run_ours(args):
                          "peak_dpx_instr_per_s": dpx, "peak_i32_instr_per_s": i32,
                          "model": "4 DPX int16x2 instructions per cell (probe measured live)"},
         "clocks": clk,
+        "batched": batched,
     }
+    if not args.no_mixed:
+        result["mixed"] = run_mixed(args, bsw, dist)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         sample = cpu_sample(wl, args.cpu_seconds, nthreads)
@@ -377,6 +404,51 @@ def run_ours(args):
     dist.close()
     if rank == 0:
         print(json.dumps(result), flush=True)
+
+
+def run_mixed(args, bsw_unused, dist):
+    """The mixed-length workload (10,000,000 pairs: lognormal query lengths
+    clipped to [20, 2000], bands 20/50/100 per pair, 8/16-bit routing per
+    pair): plain launch vs batched form on the same device-resident pairs."""
+    import torch
+    import tal_bsw
+    from tal_bsw import synth
+    wl = synth.C3
+    n = args.mixed_pairs or wl.n_pairs
+    b = synth.generate(wl, n, first=dist.rank * n)
+    P = wl.params()
+    bsw = tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                   P["end_bonus"], None, P["a"], P["b"], 1, device=dist.local)
+    dp = torch.from_numpy(b.pairs.view(np.uint8).reshape(-1).copy()).cuda()
+    dr = torch.from_numpy(b.ref).cuda()
+    dq = torch.from_numpy(b.qer).cuda()
+    dw = torch.from_numpy(b.w.astype(np.int32)).cuda()
+    del b
+    out = {"workload": f"c3_mixed: {n} pairs, lognormal query (median 120, sigma 0.8) in [20,2000], "
+                       "w per pair in {20,50,100}, 8/16-bit routed per pair"}
+    for mode, steps in (("plain", 2), ("batched", 5)):
+        def go():
+            if mode == "plain":
+                bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                                  n, 100, 0, dw.data_ptr())
+            else:
+                bsw.scores_batched_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(),
+                                          dq.numel(), n, 100, 0, dw.data_ptr())
+        go()
+        dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            go()
+        torch.cuda.synchronize()
+        t = dist.max((time.perf_counter() - t0) / steps)
+        cells = dist.sum(float(bsw.last_cells))
+        out[mode] = {"pairs_per_s": round(n * dist.ws / t, 1), "ms_per_step": round(t * 1e3, 2),
+                     "kernel_gcups": round(cells / t / 1e9, 2), "steps": steps}
+    out["batched_over_plain_pairs_per_s"] = round(out["batched"]["pairs_per_s"] /
+                                                  out["plain"]["pairs_per_s"], 2)
+    bsw.close()
+    return out
 
 
 # -------------------------------------------------------------------- reference arm
