@@ -59,6 +59,13 @@ def parse_args():
                     help="skip the mixed-length plain-vs-batched comparison")
     ap.add_argument("--mixed-pairs", type=int, default=None,
                     help="pairs of the mixed-length workload (default: all 10,000,000)")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
+    ap.add_argument("--serve-loads", type=float, nargs="+", default=[0.1, 0.3, 0.5, 0.7, 0.9])
+    ap.add_argument("--serve-requests", type=int, default=300, help="requests per load point")
+    ap.add_argument("--serve-plain-loads", type=float, nargs="+", default=[0.1, 0.7])
+    ap.add_argument("--serve-plain-requests", type=int, default=120)
+    ap.add_argument("--serve-pool-pairs", type=int, default=3_000_000,
+                    help="pairs the serving requests are drawn from")
     return ap.parse_args()
 
 
@@ -391,6 +398,9 @@ def run_ours(args):
     }
     if not args.no_mixed:
         result["mixed"] = run_mixed(args, bsw, dist)
+    if not args.no_serving:
+        peak = result.get("mixed", {}).get("batched", {}).get("pairs_per_s")
+        result["serving"] = run_serving(args, dist, peak / dist.ws if peak else None)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         sample = cpu_sample(wl, args.cpu_seconds, nthreads)
@@ -447,6 +457,163 @@ def run_mixed(args, bsw_unused, dist):
                      "kernel_gcups": round(cells / t / 1e9, 2), "steps": steps}
     out["batched_over_plain_pairs_per_s"] = round(out["batched"]["pairs_per_s"] /
                                                   out["plain"]["pairs_per_s"], 2)
+    bsw.close()
+    return out
+
+
+def run_serving(args, dist, peak_pairs_per_s):
+    """The serving loop under Poisson arrivals: requests of log-uniform size in
+    [1,000, 200,000] pairs drawn from the mixed-length distribution, offered at
+    10-90 % of the measured batched peak, against a device pool of at most
+    64 GB.  Latency of a request = its outputs in the caller's (pinned) array
+    minus its scheduled arrival time.  Beside it, the same arrivals through a
+    plain launch per request (one request at a time, FIFO)."""
+    import threading
+    import torch
+    import tal_bsw
+    from tal_bsw import synth
+    from tal_bsw.api import BswServer, now_ns
+    wl = synth.C3
+    npool = args.serve_pool_pairs
+    b = synth.generate(wl, npool, first=20_000_000 + dist.rank * npool)
+    P = wl.params()
+    bsw = tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                   P["end_bonus"], None, P["a"], P["b"], 1, device=dist.local)
+
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        v = t.numpy().view(a.dtype).reshape(a.shape)
+        v[...] = a
+        return v, t
+
+    hp, hp_t = pinned(b.pairs)
+    hr, hr_t = pinned(b.ref)
+    hq, hq_t = pinned(b.qer)
+    hw, hw_t = pinned(b.w.astype(np.int32))
+    # expected outputs (and the autotuner's bin choices) from the batched form
+    exp = b.pairs.copy()
+    bsw.scores_batched(exp, b.ref, b.qer, npool, 100, wpair=b.w, bits=tal_bsw.AUTO)
+    if not peak_pairs_per_s:
+        t0 = time.perf_counter()
+        tmp = b.pairs.copy()
+        bsw.scores_batched(tmp, b.ref, b.qer, npool, 100, wpair=b.w, bits=tal_bsw.AUTO)
+        peak_pairs_per_s = npool / (time.perf_counter() - t0)
+    lo_n, hi_n = 1000, 200000
+    mean_req = (hi_n - lo_n) / np.log(hi_n / lo_n)
+    rng = np.random.default_rng(1234 + dist.rank)
+
+    def schedule(load, nreq):
+        rate = load * peak_pairs_per_s / mean_req            # requests per second
+        gaps = rng.exponential(1.0 / rate, nreq)
+        arrive = np.cumsum(gaps) - gaps[0]
+        sizes = np.exp(rng.uniform(np.log(lo_n), np.log(hi_n), nreq)).astype(np.int64)
+        starts, cur = [], int(rng.integers(0, npool))
+        for s_ in sizes:
+            if cur + s_ > npool:
+                cur = 0
+            starts.append(cur)
+            cur += int(s_)
+        return arrive, sizes, np.array(starts)
+
+    def drive(submit, wait, arrive, sizes, starts):
+        """Submits at the scheduled times from one thread, collects in order
+        on this one; returns per-request latency (ns) and the makespan."""
+        nreq = len(sizes)
+        tickets = [None] * nreq
+        t0 = now_ns() + 20_000_000
+        sched = (t0 + arrive * 1e9).astype(np.int64)
+
+        def submitter():
+            for k in range(nreq):
+                while True:
+                    d = sched[k] - now_ns()
+                    if d <= 0:
+                        break
+                    if d > 2_000_000:
+                        time.sleep((d - 1_000_000) / 1e9)
+                tickets[k] = submit(int(starts[k]), int(sizes[k]))
+        th = threading.Thread(target=submitter)
+        th.start()
+        done = np.zeros(nreq, np.int64)
+        for k in range(nreq):
+            while tickets[k] is None:
+                time.sleep(0.0002)
+            done[k] = wait(tickets[k])
+        th.join()
+        return done - sched, done.max() - t0
+
+    out = {"workload": f"requests of log-uniform size in [{lo_n}, {hi_n}] pairs (mean {mean_req:.0f}) "
+                       f"drawn from c3_mixed ({npool} pooled pairs), Poisson arrivals",
+           "batched_peak_pairs_per_s": round(peak_pairs_per_s, 1), "points": []}
+    srv = BswServer(bsw)                       # pool: min(64 GiB, 85 % of free HBM)
+    infos = {}
+
+    def s_submit(lo, n):
+        return srv.submit(hp[lo:lo + n], hr, hq, w=100, wpair=hw[lo:lo + n], bits=tal_bsw.AUTO)
+
+    def s_wait(t):
+        info = srv.poll(t, timeout_us=600_000_000)
+        assert info is not None and info.status == 0, "serving request failed"
+        infos[t] = info
+        return info.done_ns
+    # warm-up (first ticks, staging of the worker)
+    drive(s_submit, s_wait, *schedule(0.3, 20))
+    for load in args.serve_loads:
+        nreq = args.serve_requests
+        arrive, sizes, starts = schedule(load, nreq)
+        infos.clear()
+        lat, span = drive(s_submit, s_wait, arrive, sizes, starts)
+        ticks = [i.tick_requests for i in infos.values()]
+        out["points"].append({
+            "load": load, "requests": nreq,
+            "offered_pairs_per_s": round(load * peak_pairs_per_s, 1),
+            "achieved_pairs_per_s": round(float(sizes.sum()) / (span / 1e9), 1),
+            "p50_ms": round(float(np.percentile(lat, 50)) / 1e6, 3),
+            "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3),
+            "max_ms": round(float(lat.max()) / 1e6, 3),
+            "mean_tick_requests": round(float(np.mean(ticks)), 2)})
+    # saturation: every request at once
+    arrive, sizes, starts = schedule(1.0, args.serve_requests)
+    lat, span = drive(s_submit, s_wait, np.zeros_like(arrive), sizes, starts)
+    out["saturated_pairs_per_s"] = round(float(sizes.sum()) / (span / 1e9), 1)
+    st = srv.stats()
+    srv.close()
+    out["server"] = {k: st[k] for k in ("ticks", "pairs", "max_tick_requests", "max_ticks_in_flight",
+                                        "pool_bytes", "pool_peak_bytes", "failed")}
+    out["outputs_match"] = bool((tal_bsw.outputs(hp) == tal_bsw.outputs(exp)).all())
+
+    # plain launch per request: one request at a time (FIFO), pairs copied in
+    # and out per request, sequences device-resident
+    dr = torch.from_numpy(b.ref).cuda()
+    dq = torch.from_numpy(b.qer).cuda()
+    dw = torch.from_numpy(b.w.astype(np.int32)).cuda()
+    dpair = torch.empty(hi_n * 56, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.ExternalStream(bsw.stream)
+    hp_u8 = hp_t
+
+    def p_submit(lo, n):
+        return (lo, n)
+
+    def p_wait(t):
+        lo, n = t
+        with torch.cuda.stream(stream):
+            dpair[:n * 56].copy_(hp_u8[lo * 56:(lo + n) * 56], non_blocking=True)
+        bsw.scores_device(dpair.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(), n,
+                          100, tal_bsw.AUTO, d_w=dw.data_ptr() + 4 * lo, sync=False)
+        with torch.cuda.stream(stream):
+            hp_u8[lo * 56:(lo + n) * 56].copy_(dpair[:n * 56], non_blocking=True)
+        bsw.sync()
+        return now_ns()
+    out["plain_per_request"] = []
+    for load in args.serve_plain_loads:
+        arrive, sizes, starts = schedule(load, args.serve_plain_requests)
+        lat, span = drive(p_submit, p_wait, arrive, sizes, starts)
+        out["plain_per_request"].append({
+            "load": load, "requests": len(sizes),
+            "achieved_pairs_per_s": round(float(sizes.sum()) / (span / 1e9), 1),
+            "p50_ms": round(float(np.percentile(lat, 50)) / 1e6, 3),
+            "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3)})
+    out["plain_outputs_match"] = bool((tal_bsw.outputs(hp) == tal_bsw.outputs(exp)).all())
     bsw.close()
     return out
 

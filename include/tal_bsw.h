@@ -177,6 +177,86 @@ int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_seq_pair *d_
                                   const uint8_t *d_qer, size_t qer_bytes, int32_t numPairs,
                                   int32_t w, const int32_t *d_w, int bits, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Serving loop; no counterpart in the reference, whose callers block in one
+ * getScores call per batch (bench-bsw.cpp:216-258).
+ *
+ * A server takes scoring requests -- SeqPair batches of any size, each with
+ * its own sequence buffers, band and precision -- as they arrive, and runs
+ * them with continuous batching: a worker thread admits queued requests in
+ * arrival order as soon as their pairs and sequences fit the server's device
+ * pool (admission by free device memory), copies them in while earlier work
+ * runs, and launches every admitted request that is not yet running as one
+ * "tick" (a device-side length sort of all their pairs plus one persistent
+ * launch per non-empty length bin).  Up to `slots` ticks are on the device at
+ * once, on their own streams, so a tick admitted while another runs overlaps
+ * with it.  Each request's outputs are those of tal_bsw_scores on the same
+ * pairs, alone or in any mix, and one request's bad pair fails only that
+ * request.  Caller buffers stay owned by the caller and must stay valid
+ * until the request is polled complete; pinned (page-locked) buffers are
+ * copied directly, pageable ones through the server's pinned staging. */
+typedef struct tal_bsw_server *tal_bsw_server_handle;
+
+typedef struct {
+    size_t pool_bytes;      /* device pool for requests' pairs and sequences;
+                               0 = min(64 GiB, 85% of the free device memory) */
+    size_t staging_bytes;   /* pinned host staging for pageable callers; 0 = 1 GiB */
+    int32_t max_tick_pairs; /* most pairs in one tick (and in one request);
+                               0 = 8,388,608 */
+    int32_t slots;          /* ticks on the device at once, 1..4; 0 = 2 */
+} tal_bsw_server_config;
+
+typedef struct {
+    int32_t status;          /* TAL_OK, TAL_EDOMAIN (bad_pair names the pair) or TAL_ECUDA */
+    int32_t tick_requests;   /* requests in the tick that ran this one */
+    int64_t bad_pair;        /* first offending pair of this request, or -1 */
+    int64_t tick_pairs;      /* pairs in that tick */
+    int64_t submit_ns;       /* steady-clock times (tal_bsw_now_ns): submit call, */
+    int64_t admit_ns;        /*   copies issued into the pool, */
+    int64_t launch_ns;       /*   its tick launched, */
+    int64_t done_ns;         /*   outputs in the caller's SeqPair array */
+} tal_bsw_request_info;
+
+typedef struct {
+    uint64_t submitted, completed, failed, ticks, pairs, launches;
+    uint64_t pool_bytes, pool_used_bytes, pool_peak_bytes;
+    int32_t queued, admitted, running;     /* requests in each state now */
+    int32_t max_tick_requests;             /* most requests one tick has carried */
+    int32_t max_ticks_in_flight;           /* most ticks on the device at once */
+    int32_t pad_;
+} tal_bsw_server_stats;
+
+/* Steady-clock nanoseconds, the clock of tal_bsw_request_info. */
+int64_t tal_bsw_now_ns(void);
+
+/* Creates a server with the scoring parameters of `h` and its length-bin
+ * configurations (the autotuner's, when h ran a batched call; else the
+ * defaults), on h's device.  h may be destroyed afterwards. */
+int tal_bsw_server_create(tal_bsw_handle h, const tal_bsw_server_config *cfg,
+                          tal_bsw_server_handle *out);
+
+/* Completes every submitted request, then frees the server. */
+int tal_bsw_server_destroy(tal_bsw_server_handle s);
+
+/* Queues a request: score pairs[0, numPairs) against seqBufRef / seqBufQer
+ * (offsets idr / idq as in tal_bsw_scores) with band w, or wpair[k] per pair
+ * when wpair is not NULL, and bits 8 / 16 / TAL_BSW_AUTO.  Returns at once
+ * with a ticket.  TAL_EINVAL: bad arguments or numPairs > max_tick_pairs;
+ * TAL_ENOMEM: the request can never fit the pool or the staging; TAL_EBUSY:
+ * pageable buffers and the staging is full right now (retry later). */
+int tal_bsw_submit(tal_bsw_server_handle s, tal_seq_pair *pairs, const uint8_t *seqBufRef,
+                   const uint8_t *seqBufQer, int32_t numPairs, int32_t w,
+                   const int32_t *wpair, int bits, uint64_t *ticket);
+
+/* Waits up to timeout_us (0: just checks, negative: no limit) for the
+ * request.  TAL_OK: it is complete, its outputs are in its SeqPair array,
+ * info (optional) holds its status and times, and the ticket is released.
+ * TAL_ETIMEOUT: not complete yet.  TAL_EINVAL: unknown ticket. */
+int tal_bsw_poll(tal_bsw_server_handle s, uint64_t ticket, int64_t timeout_us,
+                 tal_bsw_request_info *info);
+
+int tal_bsw_server_get_stats(tal_bsw_server_handle s, tal_bsw_server_stats *out);
+
 #ifdef __cplusplus
 }
 #endif

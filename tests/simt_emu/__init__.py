@@ -45,3 +45,40 @@ def run(pairs, ref, qer, w, params, bits=16, K=4, warps=1, wpair=None, G=32):
                      None if wp is None else vp(wp.ctypes.data), int(bits), vp(kp.ctypes.data),
                      int(G), int(K), int(warps), ctypes.byref(ef), ctypes.byref(ei))
     return out, ef.value, ei.value
+
+
+def run_reqs(reqs, order, params, K=4, warps=1, G=32):
+    """A serving tick on the emulated kernel.  reqs: list of dicts with
+    pairs, ref, qer (the request's byte windows), ref_lo, qer_lo (window
+    offsets), w, bits and optional wpair; order: list of (request, local
+    index) work items.  Returns (list of output pair arrays, err, bad)."""
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        _lib.emu_bsw_run.restype = ctypes.c_int
+    nreq = len(reqs)
+    vp = ctypes.c_void_p
+    outs = [np.ascontiguousarray(r["pairs"]).copy() for r in reqs]
+    refs = [np.ascontiguousarray(r["ref"]) for r in reqs]
+    qers = [np.ascontiguousarray(r["qer"]) for r in reqs]
+    wps = [None if r.get("wpair") is None else np.ascontiguousarray(r["wpair"], np.int32) for r in reqs]
+    P = (vp * nreq)
+    LL = (ctypes.c_longlong * nreq)
+    I = (ctypes.c_int * nreq)
+    kp = np.array([params[k] for k in ("o_del", "e_del", "o_ins", "e_ins", "zdrop", "end_bonus", "a", "b")],
+                  np.int32)
+    o = np.array([k for _, k in order], np.int32)
+    orq = np.array([r for r, _ in order], np.int32)
+    err = I()
+    bad = LL()
+    rc = _lib.emu_bsw_run_reqs(
+        nreq, P(*[o_.ctypes.data for o_ in outs]), P(*[r_.ctypes.data for r_ in refs]),
+        LL(*[r["ref_lo"] for r in reqs]), LL(*[r["ref_lo"] + refs[i].shape[0] for i, r in enumerate(reqs)]),
+        P(*[q_.ctypes.data for q_ in qers]),
+        LL(*[r["qer_lo"] for r in reqs]), LL(*[r["qer_lo"] + qers[i].shape[0] for i, r in enumerate(reqs)]),
+        P(*[None if x is None else x.ctypes.data for x in wps]),
+        I(*[int(x.shape[0]) for x in outs]), I(*[int(r["w"]) for r in reqs]),
+        I(*[int(r["bits"]) for r in reqs]), int(o.shape[0]), vp(o.ctypes.data), vp(orq.ctypes.data),
+        vp(kp.ctypes.data), int(G), int(K), int(warps), err, bad)
+    assert rc == 0, "lanes of a warp exited apart"
+    return outs, list(err), list(bad)

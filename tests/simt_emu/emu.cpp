@@ -21,25 +21,9 @@ std::mutex atomic_mu;
 #include "bsw_lane.cuh"
 #include <functional>
 
-extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long ref_lo,
-                           long long ref_hi, const uint8_t *qer, long long qer_lo,
-                           long long qer_hi, int n, int w, const int32_t *wpair, int bits,
-                           const int32_t *kp, int G, int K, int warps, int *err_flags,
-                           long long *err_index) {
-    talbsw::LaunchArgs A;
-    std::memset(&A, 0, sizeof(A));
-    A.pairs = pairs;
-    A.ref = ref; A.ref_lo = ref_lo; A.ref_hi = ref_hi;
-    A.qer = qer; A.qer_lo = qer_lo; A.qer_hi = qer_hi;
-    A.wpair = wpair;
-    A.n = n; A.w = w; A.bits = bits;
-    int m1 = 1, m2 = 1;
-    for (int i = 0; i < n; i++) { m1 = std::max(m1, pairs[i].len1); m2 = std::max(m2, pairs[i].len2); }
-    A.cols_cap = m2; A.rows_cap = m1;
-    int counter = 0;
-    *err_flags = 0; *err_index = (long long)INT64_MAX;
-    A.work_counter = &counter; A.err_flags = err_flags; A.err_index = err_index;
-    A.P = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], kp[6], kp[7]};
+// Runs one launch of A (one block of `warps` warps); -1 if a warp's lanes
+// did not finish together (a divergent exit).
+static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps) {
     size_t wbytes = G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap)
                            : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G);
     std::vector<unsigned char> smem(wbytes * warps + 64, 0xA5);  // poisoned, like fresh smem
@@ -94,4 +78,71 @@ extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long
     }
     if (divergent) return -1;
     return 0;
+}
+
+extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long ref_lo,
+                           long long ref_hi, const uint8_t *qer, long long qer_lo,
+                           long long qer_hi, int n, int w, const int32_t *wpair, int bits,
+                           const int32_t *kp, int G, int K, int warps, int *err_flags,
+                           long long *err_index) {
+    talbsw::LaunchArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.pairs = pairs;
+    A.ref = ref; A.ref_lo = ref_lo; A.ref_hi = ref_hi;
+    A.qer = qer; A.qer_lo = qer_lo; A.qer_hi = qer_hi;
+    A.wpair = wpair;
+    A.n = n; A.w = w; A.bits = bits;
+    int m1 = 1, m2 = 1;
+    for (int i = 0; i < n; i++) { m1 = std::max(m1, pairs[i].len1); m2 = std::max(m2, pairs[i].len2); }
+    A.cols_cap = m2; A.rows_cap = m1;
+    int counter = 0;
+    *err_flags = 0; *err_index = (long long)INT64_MAX;
+    A.work_counter = &counter; A.err_flags = err_flags; A.err_index = err_index;
+    A.P = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], kp[6], kp[7]};
+    return run_launch(A, G, K, warps);
+}
+
+// A serving tick: nreq requests, each with its own pair array, sequence
+// windows, band and precision, scored in the work order given by
+// order (request-local index) / order_req (request).  Per request errors go
+// to req_err / req_bad.
+extern "C" int emu_bsw_run_reqs(int nreq, talbsw::DevPair **pairs, const uint8_t **ref,
+                                const long long *ref_lo, const long long *ref_hi,
+                                const uint8_t **qer, const long long *qer_lo,
+                                const long long *qer_hi, const int32_t **wpair, const int *n,
+                                const int *w, const int *bits, int nwork, const int32_t *order,
+                                const int32_t *order_req, const int32_t *kp, int G, int K,
+                                int warps, int *req_err, long long *req_bad) {
+    std::vector<talbsw::ReqDesc> R(nreq);
+    int first = 0, m1 = 1, m2 = 1;
+    for (int r = 0; r < nreq; r++) {
+        talbsw::ReqDesc &d = R[r];
+        std::memset(&d, 0, sizeof(d));
+        d.pairs = pairs[r]; d.ref = ref[r]; d.qer = qer[r]; d.wpair = wpair[r];
+        d.ref_lo = ref_lo[r]; d.ref_hi = ref_hi[r]; d.qer_lo = qer_lo[r]; d.qer_hi = qer_hi[r];
+        d.bad = (long long)INT64_MAX;
+        d.first = first; d.n = n[r]; d.w = w[r]; d.bits = bits[r];
+        first += n[r];
+        for (int k = 0; k < n[r]; k++) {
+            m1 = std::max(m1, pairs[r][k].len1);
+            m2 = std::max(m2, pairs[r][k].len2);
+        }
+    }
+    talbsw::LaunchArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.reqs = R.data();
+    A.order = order;
+    A.order_req = order_req;
+    A.n = nwork;
+    A.cols_cap = m2; A.rows_cap = m1;
+    int counter = 0, flags = 0;
+    long long bad = (long long)INT64_MAX;
+    A.work_counter = &counter; A.err_flags = &flags; A.err_index = &bad;
+    A.P = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], kp[6], kp[7]};
+    const int rc = run_launch(A, G, K, warps);
+    for (int r = 0; r < nreq; r++) {
+        req_err[r] = R[r].err;
+        req_bad[r] = R[r].bad;
+    }
+    return rc;
 }

@@ -60,3 +60,30 @@ def test_bad_params_rejected_before_device():
     p = tal_bsw.api._Params(6, 0, 6, 1, 100, 5, 1, 4)   # e_del = 0
     h = ctypes.c_void_p()
     assert lib.tal_bsw_create(ctypes.byref(p), 0, ctypes.byref(h)) == tal_bsw.api.TAL_EINVAL
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The Python mirrors of the serving structs have the C layout (sizes and
+    field offsets as gcc lays out include/tal_bsw.h)."""
+    import subprocess
+    from tal_bsw.api import RequestInfo, ServerConfig, ServerStats, _Params
+    structs = {"tal_bsw_server_config": ServerConfig, "tal_bsw_request_info": RequestInfo,
+               "tal_bsw_server_stats": ServerStats, "tal_bsw_params": _Params}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "tal_bsw.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)])
+    got = {}
+    for line in subprocess.check_output([str(exe)]).decode().splitlines():
+        c, f, v = line.split()
+        got[(c, f)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)

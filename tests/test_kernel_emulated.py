@@ -34,3 +34,51 @@ def test_emulated_kernel_matches_golden(f):
     e, g = outputs(d["expected"][:n]), outputs(got)
     bad = np.nonzero((e != g).any(1))[0]
     assert bad.size == 0, f"G={G} K={K}: pair {bad[0]}: emu {g[bad[0]].tolist()} ref {e[bad[0]].tolist()}"
+
+
+def _request(name, lo, hi, **over):
+    """Pairs [lo, hi) of a golden fixture as one serving request: its own
+    copies of the byte windows its pairs reference, its band and precision."""
+    d = np.load(os.path.join(GOLDEN, name))
+    p = d["inputs"][lo:hi].copy()
+    rlo = int(p["idr"].min()) & ~15
+    qlo = int(p["idq"].min()) & ~15
+    rhi = int((p["idr"] + p["len1"]).max())
+    qhi = int((p["idq"] + p["len2"]).max())
+    w = d["w"]
+    req = dict(pairs=p, ref=d["ref"][rlo:rhi].copy(), qer=d["qer"][qlo:qhi].copy(), ref_lo=rlo,
+               qer_lo=qlo, bits=int(d["bits"]), expected=d["expected"][lo:hi])
+    if np.ndim(w):
+        req.update(w=0, wpair=w[lo:hi].astype(np.int32))
+    else:
+        req.update(w=int(w))
+    req.update(over)
+    return req
+
+
+@pytest.mark.parametrize("G,K", [(1, 4), (8, 4)])
+def test_emulated_request_table(G, K):
+    """A serving tick: pairs of five requests (8-bit, 16-bit, per-pair band
+    with routing, narrow bands) interleaved in one work list, each request with
+    its own buffers; one more request holds a bad pair.  Every good request
+    gets the reference's outputs and no error; only the bad request is flagged,
+    with its own local index."""
+    reqs = [_request("wl_c1_8bit.npz", 0, 9), _request("wl_c2_16bit.npz", 5, 13),
+            _request("wl_c3_mixed.npz", 40, 52), _request("edge16_band_3.npz", 0, 7),
+            _request("edge8_band_17.npz", 3, 10)]
+    bad = _request("wl_c2_16bit.npz", 20, 26)
+    bad["pairs"]["len1"][3] = -1           # outside the exact range: TAL_EDOMAIN
+    reqs.append(bad)
+    P = dict(o_del=6, e_del=1, o_ins=6, e_ins=1, zdrop=100, end_bonus=5, a=1, b=4)
+    items = [(r, k) for r, q in enumerate(reqs) for k in range(q["pairs"].shape[0])]
+    rng = np.random.default_rng(11)
+    order = [items[i] for i in rng.permutation(len(items))]
+    outs, err, badidx = simt_emu.run_reqs(reqs, order, P, K=K, warps=2, G=G)
+    for r, q in enumerate(reqs[:-1]):
+        assert err[r] == 0
+        e, g = outputs(q["expected"]), outputs(outs[r])
+        diff = np.nonzero((e != g).any(1))[0]
+        assert diff.size == 0, f"request {r} pair {diff[0]}: {g[diff[0]].tolist()} vs {e[diff[0]].tolist()}"
+    assert err[-1] != 0 and badidx[-1] == 3
+    keep = [k for k in range(6) if k != 3]
+    assert (outputs(outs[-1])[keep] == outputs(bad["expected"])[keep]).all()

@@ -34,6 +34,27 @@ __device__ __forceinline__ int bucket_of(const DevPair &p) {
     return bin_of(p.len2) * kRowBuckets + r;
 }
 
+// Pair k of the work list: of the launch's pair array, or -- for a serving
+// tick -- of the request whose range [first, first + n) holds k (binary
+// search over the tick's request table).
+__device__ __forceinline__ const DevPair &pair_of(const DevPair *p, const ReqDesc *reqs, int nreqs,
+                                                  int k, int &req, int &local) {
+    if (!reqs) {
+        req = -1;
+        local = k;
+        return p[k];
+    }
+    int lo = 0, hi = nreqs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (reqs[mid].first <= k) lo = mid;
+        else hi = mid - 1;
+    }
+    req = lo;
+    local = k - reqs[lo].first;
+    return reqs[lo].pairs[local];
+}
+
 __global__ void batch_init_kernel(BatchCtrl *c) {
     for (int k = threadIdx.x; k <= kNumBins; k += blockDim.x) c->counter[k] = 0;
     if (threadIdx.x == 0) {
@@ -44,13 +65,15 @@ __global__ void batch_init_kernel(BatchCtrl *c) {
 }
 
 // bucket histogram, one atomic per distinct bucket per warp
-__global__ void batch_hist_kernel(const DevPair *p, int n, int *counts) {
+__global__ void batch_hist_kernel(const DevPair *p, const ReqDesc *reqs, int nreqs, int n,
+                                  int *counts) {
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int k = base + threadIdx.x;
         const bool valid = k < n;
         const unsigned act = __ballot_sync(0xffffffffu, valid);
         if (!valid) continue;
-        const int key = bucket_of(p[k]);
+        int req, local;
+        const int key = bucket_of(pair_of(p, reqs, nreqs, k, req, local));
         const unsigned m = __match_any_sync(act, key);
         if ((int)(threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(counts + key, __popc(m));
     }
@@ -105,14 +128,16 @@ __global__ void __launch_bounds__(1024) batch_scan_kernel(int *counts, int *seg)
 
 // scatter pair indices into bucket order; within a bin the order is reversed
 // so the longest targets come first
-__global__ void batch_scatter_kernel(const DevPair *p, int n, int *cursor, const int *seg,
-                                     int32_t *order) {
+__global__ void batch_scatter_kernel(const DevPair *p, const ReqDesc *reqs, int nreqs, int n,
+                                     int *cursor, const int *seg, int32_t *order,
+                                     int32_t *order_req) {
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int k = base + threadIdx.x;
         const bool valid = k < n;
         const unsigned act = __ballot_sync(0xffffffffu, valid);
         if (!valid) continue;
-        const int key = bucket_of(p[k]);
+        int req, local;
+        const int key = bucket_of(pair_of(p, reqs, nreqs, k, req, local));
         const unsigned m = __match_any_sync(act, key);
         const int lane = threadIdx.x & 31;
         const int leader = __ffs(m) - 1;
@@ -122,7 +147,8 @@ __global__ void batch_scatter_kernel(const DevPair *p, int n, int *cursor, const
         const int pos = b0 + __popc(m & ((1u << lane) - 1u));
         const int bin = key / kRowBuckets;
         const int s0 = seg[2 * bin], s1 = s0 + seg[2 * bin + 1];
-        order[s0 + s1 - 1 - pos] = k;
+        order[s0 + s1 - 1 - pos] = local;
+        if (order_req) order_req[s0 + s1 - 1 - pos] = req;
     }
 }
 
@@ -137,22 +163,24 @@ int bfail(tal_bsw_ctx *h, int code, const std::string &msg) {
     return code;
 }
 
-// Row capacity of a bin: its query-length bound, within shared memory.
-int bin_cols(const tal_bsw_ctx *h, int b) {
-    int c = bin_upper(b);
-    // the widest one-pair-per-warp configuration must fit the block limit
-    while (c > 32 && warp_smem_bytes(c, 1, 32) > h->smem_optin) c -= 512;
-    return c;
-}
-
 KConfig default_cfg(const tal_bsw_ctx *h, int b, int w) {
     return fit_config(choose_config(w, bin_cols(h, b)), bin_cols(h, b), h->smem_optin);
+}
+
+
+SortBufs handle_sort_bufs(tal_bsw_ctx *h) {
+    SortBufs sb;
+    sb.counts = reinterpret_cast<int *>(h->bcounts.p);
+    sb.order = reinterpret_cast<int32_t *>(h->border.p);
+    sb.order_req = nullptr;
+    sb.seg = reinterpret_cast<int32_t *>(h->bseg.p);
+    sb.ctrl = reinterpret_cast<BatchCtrl *>(h->bctrl.p);
+    return sb;
 }
 
 LaunchArgs bin_args(tal_bsw_ctx *h, int b, DevPair *pairs, const uint8_t *ref, size_t ref_bytes,
                     const uint8_t *qer, size_t qer_bytes, int n, int w, const int32_t *d_w, int bits,
                     const int32_t *seg) {
-    BatchCtrl *c = reinterpret_cast<BatchCtrl *>(h->bctrl.p);
     LaunchArgs A;
     memset(&A, 0, sizeof(A));
     A.pairs = pairs;
@@ -160,37 +188,66 @@ LaunchArgs bin_args(tal_bsw_ctx *h, int b, DevPair *pairs, const uint8_t *ref, s
     A.qer = qer;
     A.ref_lo = 0; A.ref_hi = (long long)ref_bytes;
     A.qer_lo = 0; A.qer_hi = (long long)qer_bytes;
-    A.order = reinterpret_cast<const int32_t *>(h->border.p);
-    A.seg = seg;
     A.wpair = d_w;
-    A.n = n;  // upper bound, sizes the persistent grid
     A.w = w;
     A.bits = bits;
+    return bin_launch_args(h, handle_sort_bufs(h), A, b, n, seg);
+}
+
+}  // namespace
+
+namespace talbsw {
+
+// The per-bin fields of a launch over a sorted work list: row capacity, the
+// bin's {offset, count}, its work counter, the control block.
+LaunchArgs bin_launch_args(const tal_bsw_ctx *h, const SortBufs &sb, LaunchArgs A, int b, int n,
+                           const int32_t *seg) {
+    A.order = sb.order;
+    A.order_req = sb.order_req;
+    A.seg = seg;
+    A.n = n;  // upper bound, sizes the persistent grid
     A.cols_cap = bin_cols(h, b);
     A.rows_cap = 1;
-    A.work_counter = &c->counter[b];
-    A.err_flags = &c->flags;
-    A.err_index = &c->bad_index;
-    A.cells = &c->cells;
+    A.work_counter = &sb.ctrl->counter[b];
+    A.err_flags = &sb.ctrl->flags;
+    A.err_index = &sb.ctrl->bad_index;
+    A.cells = &sb.ctrl->cells;
     A.P = h->kp;
     return A;
 }
 
-// memsets + sort kernels on the handle's stream
-cudaError_t enqueue_sort(tal_bsw_ctx *h, DevPair *pairs, int n) {
-    cudaError_t e = cudaMemsetAsync(h->bcounts.p, 0, sizeof(int) * kNumBuckets, h->stream);
+// Memset + sort kernels: bucket histogram, scan into bin segments, scatter
+// into the sorted order.  reqs (device table of nreqs requests) replaces
+// pairs for a serving tick.
+cudaError_t enqueue_sort(tal_bsw_ctx *h, const SortBufs &sb, const DevPair *pairs,
+                         const ReqDesc *reqs, int nreqs, int n, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(sb.counts, 0, sizeof(int) * kNumBuckets, s);
     if (e != cudaSuccess) return e;
-    batch_init_kernel<<<1, 64, 0, h->stream>>>(reinterpret_cast<BatchCtrl *>(h->bctrl.p));
+    batch_init_kernel<<<1, 64, 0, s>>>(sb.ctrl);
     const int blocks = (int)std::min<long long>(((long long)n + 255) / 256, (long long)h->num_sms * 8);
-    batch_hist_kernel<<<blocks, 256, 0, h->stream>>>(pairs, n, reinterpret_cast<int *>(h->bcounts.p));
-    batch_scan_kernel<<<1, 1024, 0, h->stream>>>(reinterpret_cast<int *>(h->bcounts.p),
-                                                 reinterpret_cast<int *>(h->bseg.p));
-    batch_scatter_kernel<<<blocks, 256, 0, h->stream>>>(pairs, n, reinterpret_cast<int *>(h->bcounts.p),
-                                                        reinterpret_cast<const int *>(h->bseg.p),
-                                                        reinterpret_cast<int32_t *>(h->border.p));
+    batch_hist_kernel<<<blocks, 256, 0, s>>>(pairs, reqs, nreqs, n, sb.counts);
+    batch_scan_kernel<<<1, 1024, 0, s>>>(sb.counts, sb.seg);
+    batch_scatter_kernel<<<blocks, 256, 0, s>>>(pairs, reqs, nreqs, n, sb.counts, sb.seg, sb.order,
+                                                sb.order_req);
     h->launches += 4;
     return cudaGetLastError();
 }
+
+KConfig bin_kconfig(const tal_bsw_ctx *h, int b, int w) {
+    if (h->tuned) return h->bin_cfg[b];
+    return fit_config(choose_config(w, bin_cols(h, b)), bin_cols(h, b), h->smem_optin);
+}
+
+int bin_cols(const tal_bsw_ctx *h, int b) {
+    int c = bin_upper(b);
+    // the widest one-pair-per-warp configuration must fit the block limit
+    while (c > 32 && warp_smem_bytes(c, 1, 32) > h->smem_optin) c -= 512;
+    return c;
+}
+
+}  // namespace talbsw
+
+namespace {
 
 cudaError_t enqueue_bins(tal_bsw_ctx *h, DevPair *pairs, const uint8_t *ref, size_t ref_bytes,
                          const uint8_t *qer, size_t qer_bytes, int n, int w, const int32_t *d_w,
@@ -210,7 +267,7 @@ cudaError_t enqueue_bins(tal_bsw_ctx *h, DevPair *pairs, const uint8_t *ref, siz
 int autotune(tal_bsw_ctx *h, DevPair *pairs, const uint8_t *ref, size_t ref_bytes,
              const uint8_t *qer, size_t qer_bytes, int n, int w, const int32_t *d_w, int bits) {
     constexpr int kSample = 16384;
-    cudaError_t e = enqueue_sort(h, pairs, n);
+    cudaError_t e = enqueue_sort(h, handle_sort_bufs(h), pairs, nullptr, 0, n, h->stream);
     int seg[2 * kNumBins];
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(seg, h->bseg.p, sizeof(seg), cudaMemcpyDeviceToHost, h->stream);
@@ -317,7 +374,8 @@ int batched_device_locked(tal_bsw_ctx *h, tal_seq_pair *d_pairs, const uint8_t *
         cudaGraph_t g = nullptr;
         e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaError_t e1 = enqueue_sort(h, pairs, numPairs);
+            cudaError_t e1 = enqueue_sort(h, handle_sort_bufs(h), pairs, nullptr, 0, numPairs,
+                                          h->stream);
             cudaError_t e2 = e1 == cudaSuccess
                                  ? enqueue_bins(h, pairs, d_ref, ref_bytes, d_qer, qer_bytes,
                                                 numPairs, w, d_w, bits)

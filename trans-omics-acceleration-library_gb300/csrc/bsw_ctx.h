@@ -68,6 +68,31 @@ struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
 };
 
+// Device buffers of one sort: bucket counts (kNumBuckets), sorted order and
+// -- for a serving tick -- the request of each sorted item, bin segments
+// {offset, count} x kNumBins, control block.
+struct SortBufs {
+    int *counts;
+    int32_t *order;
+    int32_t *order_req;
+    int32_t *seg;
+    BatchCtrl *ctrl;
+};
+
+}  // namespace talbsw
+
+struct tal_bsw_ctx;
+
+namespace talbsw {
+// Implemented in bsw_batched.cu; used by the serving loop (bsw_serve.cu).
+int bin_cols(const tal_bsw_ctx *h, int b);
+// Kernel and tile of length bin b: the autotuner's choice, else the default
+// for band w.
+KConfig bin_kconfig(const tal_bsw_ctx *h, int b, int w);
+LaunchArgs bin_launch_args(const tal_bsw_ctx *h, const SortBufs &sb, LaunchArgs A, int b, int n,
+                           const int32_t *seg);
+cudaError_t enqueue_sort(tal_bsw_ctx *h, const SortBufs &sb, const DevPair *pairs,
+                         const ReqDesc *reqs, int nreqs, int n, cudaStream_t s);
 }  // namespace talbsw
 
 struct tal_bsw_ctx {

@@ -59,6 +59,23 @@ struct DevPair {  // SeqPair, bandedSWA.h:90-99
 // index is recorded separately with atomicMin.
 enum : int { ERR_DOMAIN = 1, ERR_CAPACITY = 2, ERR_BASE = 4 };
 
+// One request of a serving tick: the tick's pairs are the concatenation of
+// its requests' pair arrays, each request with its own sequence buffers,
+// band and precision.  Pair `first + k` of the tick is pair k of the request.
+// The kernels record errors per request here (err, bad), so that one
+// request's bad pair does not fail the others.
+struct ReqDesc {
+    DevPair *pairs;
+    const uint8_t *ref;
+    const uint8_t *qer;
+    const int32_t *wpair;     // optional per-pair band
+    long long ref_lo, ref_hi, qer_lo, qer_hi;
+    long long bad;            // first offending pair, request-local (LLONG_MAX if none)
+    int first, n, w, bits;
+    int err;                  // ERR_* flags
+    int pad_;
+};
+
 struct LaunchArgs {
     DevPair *pairs;
     // ref / qer point at a device copy of the caller's buffer window
@@ -78,7 +95,52 @@ struct LaunchArgs {
     int *err_flags;
     long long *err_index;
     KernelParams P;
+    // serving tick: when reqs is set, order[] holds request-local pair
+    // indices and order_req[] (parallel to order) the request of each;
+    // pairs / ref / qer / wpair / w / bits above are unused
+    ReqDesc *reqs;
+    const int32_t *order_req;
 };
+
+// Where one pair's record, sequences, band and precision live.
+struct PairSrc {
+    DevPair *pp;
+    const uint8_t *ref, *qer;
+    long long ref_lo, ref_hi, qer_lo, qer_hi;
+    int w, bits;
+};
+
+// item: position in the (optionally sorted) work list; pidx: the pair's
+// index (request-local for a serving tick); req: its request or -1.
+__device__ __forceinline__ PairSrc pair_src(const LaunchArgs &A, int pidx, int req) {
+    PairSrc s;
+    if (req >= 0) {
+        const ReqDesc &d = A.reqs[req];
+        s.pp = d.pairs + pidx;
+        s.ref = d.ref; s.qer = d.qer;
+        s.ref_lo = d.ref_lo; s.ref_hi = d.ref_hi; s.qer_lo = d.qer_lo; s.qer_hi = d.qer_hi;
+        s.w = d.wpair ? d.wpair[pidx] : d.w;
+        s.bits = d.bits;
+    } else {
+        s.pp = A.pairs + pidx;
+        s.ref = A.ref; s.qer = A.qer;
+        s.ref_lo = A.ref_lo; s.ref_hi = A.ref_hi; s.qer_lo = A.qer_lo; s.qer_hi = A.qer_hi;
+        s.w = A.wpair ? A.wpair[pidx] : A.w;
+        s.bits = A.bits;
+    }
+    return s;
+}
+
+// Records an error for pair pidx (of request req, or of the launch).
+__device__ __forceinline__ void report_error(const LaunchArgs &A, int req, int flag, int pidx) {
+    atomicOr(A.err_flags, flag);
+    if (req >= 0) {
+        atomicOr(&A.reqs[req].err, flag);
+        atomicMin(&A.reqs[req].bad, (long long)pidx);
+    } else {
+        atomicMin(A.err_index, (long long)pidx);
+    }
+}
 
 // Element-width wrap of the reference's per-row int16 / int8 arithmetic,
 // emulated exactly: sh = 16 (int16) or 24 (int8), msk = 0xffff or 0xff.
@@ -415,7 +477,8 @@ __device__ __forceinline__ int scan_last_nz(const int *Hh, const int *Fv, int lo
 
 // Per-pair state, uniform across the pair's G lanes.
 struct PairState {
-    int pidx, nrow, ncol, i;
+    DevPair *pp;
+    int pidx, req, nrow, ncol, i;
     int beg, end, nbeg, nend, head, tail;
     int maxScore, x, y, gscore, max_ie, max_off;
     int h0e, o_delE, e_delE, bandE, wk, qlenE, mlen, zdropE;
@@ -457,14 +520,15 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
     const int oe_ins = P.o_ins + P.e_ins;
 
     PairState ps;
-    ps.pidx = 0; ps.nrow = 0; ps.ncol = 0; ps.i = 0; ps.ncells = 0;
+    ps.pidx = 0; ps.req = -1; ps.pp = nullptr; ps.nrow = 0; ps.ncol = 0; ps.i = 0; ps.ncells = 0;
     bool active = false, done = false;
     const int nwork = A.seg ? A.seg[1] : A.n;
     const int32_t *order = A.seg ? A.order + A.seg[0] : A.order;
+    const int32_t *order_req = A.reqs ? (A.seg ? A.order_req + A.seg[0] : A.order_req) : nullptr;
 
     auto finish = [&]() {
         if (gl == 0) {
-            DevPair *pp = A.pairs + ps.pidx;
+            DevPair *pp = ps.pp;
             if (A.cells) atomicAdd(A.cells, ps.ncells);
             pp->score = ps.maxScore;
             pp->tle = ps.x;
@@ -485,52 +549,47 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             item = __shfl_sync(full, item, gshift);
             const bool take = need && item < nwork;
             if (need && !take) done = true;
-            int len1 = 0, len2 = 0, h0in = 0, idr = 0, idq = 0, wcall = 0, pidx = 0;
+            int len1 = 0, len2 = 0, h0in = 0, idr = 0, idq = 0, wcall = 0, pidx = 0, req = -1;
             bool is8 = false, ok = false;
+            PairSrc src = {};
             if (take) {
                 pidx = order ? order[item] : item;
-                const DevPair *pp = A.pairs + pidx;
+                req = order_req ? order_req[item] : -1;
+                src = pair_src(A, pidx, req);
+                const DevPair *pp = src.pp;
                 len1 = pp->len1; len2 = pp->len2; h0in = pp->h0;
                 idr = pp->idr; idq = pp->idq;
-                wcall = A.wpair ? A.wpair[pidx] : A.w;
-                if (A.bits == 8) is8 = true;
-                else if (A.bits == 16) is8 = false;
+                wcall = src.w;
+                if (src.bits == 8) is8 = true;
+                else if (src.bits == 16) is8 = false;
                 else is8 = pair_in_range(P, len1, len2, h0in, wcall, true);
                 ok = pair_in_range(P, len1, len2, h0in, wcall, is8) && wcall >= 0 &&
-                     (long long)idr >= A.ref_lo && (long long)idq >= A.qer_lo &&
-                     (long long)idr + len1 <= A.ref_hi && (long long)idq + len2 <= A.qer_hi;
+                     (long long)idr >= src.ref_lo && (long long)idq >= src.qer_lo &&
+                     (long long)idr + len1 <= src.ref_hi && (long long)idq + len2 <= src.qer_hi;
                 if (!ok) {
-                    if (gl == 0) {
-                        atomicOr(A.err_flags, ERR_DOMAIN);
-                        atomicMin(A.err_index, (long long)pidx);
-                    }
+                    if (gl == 0) report_error(A, req, ERR_DOMAIN, pidx);
                 } else if (len2 > A.cols_cap) {
                     ok = false;
-                    if (gl == 0) {
-                        atomicOr(A.err_flags, ERR_CAPACITY);
-                        atomicMin(A.err_index, (long long)pidx);
-                    }
+                    if (gl == 0) report_error(A, req, ERR_CAPACITY, pidx);
                 }
             }
             bool st = take && ok;
             // stage the bases (query as PRMT selectors)
             bool bad = stage_bases<G, uint16_t, 0x1111u, 0x8880u>(
-                Qs, A.qer, st ? len2 : 0, (size_t)(A.qer_hi - A.qer_lo),
-                st ? (size_t)(idq - A.qer_lo) : 0, gl);
+                Qs, src.qer, st ? len2 : 0, (size_t)(src.qer_hi - src.qer_lo),
+                st ? (size_t)(idq - src.qer_lo) : 0, gl);
             const unsigned bm = __ballot_sync(full, bad) & gbits;
             if (st && bm) {
-                if (gl == 0) {
-                    atomicOr(A.err_flags, ERR_BASE);
-                    atomicMin(A.err_index, (long long)pidx);
-                }
+                if (gl == 0) report_error(A, req, ERR_BASE, pidx);
                 st = false;
             }
             if (st) {
                 // per-pair constants (smithWatermanBatchWrapper16/8 set-up)
                 const int sh = is8 ? 24 : 16, msk = is8 ? 0xff : 0xffff;
                 ps.is8 = is8; ps.sh = sh; ps.msk = msk;
-                ps.pidx = pidx; ps.nrow = len1; ps.ncol = len2; ps.i = 0; ps.ncells = 0;
-                Tg = A.ref + (idr - A.ref_lo);
+                ps.pidx = pidx; ps.req = req; ps.pp = src.pp;
+                ps.nrow = len1; ps.ncol = len2; ps.i = 0; ps.ncells = 0;
+                Tg = src.ref + (idr - src.ref_lo);
                 tnext = len1 > 0 ? Tg[0] : 0;
                 ps.h0e = wrapS(wrapU(h0in, msk), sh);
                 ps.o_delE = P.o_del;
@@ -629,10 +688,7 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             const int tb = rowact ? tnext : 0;
             if (rowact && i + 1 < ps.nrow) tnext = Tg[i + 1];
             if (rowact && tb > 4) {  // a target base code above 4
-                if (gl == 0) {
-                    atomicOr(A.err_flags, ERR_BASE);
-                    atomicMin(A.err_index, (long long)ps.pidx);
-                }
+                if (gl == 0) report_error(A, ps.req, ERR_BASE, ps.pidx);
                 active = false;
                 rowact = false;
             }

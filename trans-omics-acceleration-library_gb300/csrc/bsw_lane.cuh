@@ -104,6 +104,7 @@ __device__ __forceinline__ void lane_group4(uint32_t *hp, int j, uint32_t w0, ui
 struct LanePair {
     DevPair *pp;
     const uint8_t *q, *t;
+    int pidx, req;
     int nrow, ncol, i, initc, tnext;
     int head, tail, nbeg, nend;
     int maxScore, x, y, gscore, max_off, max_ie;
@@ -132,10 +133,8 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
     bool active = false;
     const int nwork = A.seg ? A.seg[1] : A.n;
     const int32_t *order = A.seg ? A.order + A.seg[0] : A.order;
-    auto fail = [&](int flag, int pidx) {
-        atomicOr(A.err_flags, flag);
-        atomicMin(A.err_index, (long long)pidx);
-    };
+    const int32_t *order_req = A.reqs ? (A.seg ? A.order_req + A.seg[0] : A.order_req) : nullptr;
+    auto fail = [&](int flag, int req, int pidx) { report_error(A, req, flag, pidx); };
     auto finish = [&]() {
         if (A.cells) atomicAdd(A.cells, s.ncells);
         s.pp->score = s.maxScore;
@@ -155,23 +154,27 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             const int item = atomicAdd(A.work_counter, 1);
             if (item >= nwork) break;
             const int pidx = order ? order[item] : item;
-            DevPair *pp = A.pairs + pidx;
+            const int req = order_req ? order_req[item] : -1;
+            const PairSrc src = pair_src(A, pidx, req);
+            DevPair *pp = src.pp;
             const int len1 = pp->len1, len2 = pp->len2, h0in = pp->h0;
             const int idr = pp->idr, idq = pp->idq;
-            const int wcall = A.wpair ? A.wpair[pidx] : A.w;
+            const int wcall = src.w;
             bool is8;
-            if (A.bits == 8) is8 = true;
-            else if (A.bits == 16) is8 = false;
+            if (src.bits == 8) is8 = true;
+            else if (src.bits == 16) is8 = false;
             else is8 = pair_in_range(P, len1, len2, h0in, wcall, true);
             const bool ok = pair_in_range(P, len1, len2, h0in, wcall, is8) && wcall >= 0 &&
-                            (long long)idr >= A.ref_lo && (long long)idq >= A.qer_lo &&
-                            (long long)idr + len1 <= A.ref_hi && (long long)idq + len2 <= A.qer_hi;
-            if (!ok) { fail(ERR_DOMAIN, pidx); continue; }
-            if (len2 > A.cols_cap) { fail(ERR_CAPACITY, pidx); continue; }
+                            (long long)idr >= src.ref_lo && (long long)idq >= src.qer_lo &&
+                            (long long)idr + len1 <= src.ref_hi && (long long)idq + len2 <= src.qer_hi;
+            if (!ok) { fail(ERR_DOMAIN, req, pidx); continue; }
+            if (len2 > A.cols_cap) { fail(ERR_CAPACITY, req, pidx); continue; }
             // per-pair constants (smithWatermanBatchWrapper16/8 set-up)
             s.pp = pp;
-            s.q = A.qer + (idq - A.qer_lo);
-            s.t = A.ref + (idr - A.ref_lo);
+            s.pidx = pidx;
+            s.req = req;
+            s.q = src.qer + (idq - src.qer_lo);
+            s.t = src.ref + (idr - src.ref_lo);
             s.nrow = len1; s.ncol = len2; s.i = 0; s.initc = 0; s.ncells = 0;
             s.is8 = is8;
             s.sh = is8 ? 24 : 16;
@@ -215,7 +218,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         const int i = s.i, ncol = s.ncol;
         const int i1 = wrapS(i + 1, sh);
         const int tb = s.tnext;
-        if (tb > 4) { fail(ERR_BASE, (int)(s.pp - A.pairs)); active = false; continue; }
+        if (tb > 4) { fail(ERR_BASE, s.req, s.pidx); active = false; continue; }
         if (i + 1 < s.nrow) s.tnext = s.t[i + 1];
         // columns up to i + wk + 3 can be touched by this row (band end + 2):
         // give them their row-0 values and stage their query selectors now
@@ -241,7 +244,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                 }
             }
             if (lim + 1 > s.initc) s.initc = lim + 1;
-            if (bad) { fail(ERR_BASE, (int)(s.pp - A.pairs)); active = false; continue; }
+            if (bad) { fail(ERR_BASE, s.req, s.pidx); active = false; continue; }
         }
         int beg = s.nbeg, end = s.nend;
         if (beg < i - s.wk) beg = i - s.wk;

@@ -65,7 +65,42 @@ _SIGS = {
                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "tal_bsw_probe_int_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_double)]),
+    "tal_bsw_now_ns": (ctypes.c_int64, []),
+    "tal_bsw_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "tal_bsw_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tal_bsw_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_uint64)]),
+    "tal_bsw_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p]),
+    "tal_bsw_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
 }
+
+
+class ServerConfig(ctypes.Structure):
+    """tal_bsw_server_config; zero fields take the library's defaults."""
+    _fields_ = [("pool_bytes", ctypes.c_size_t), ("staging_bytes", ctypes.c_size_t),
+                ("max_tick_pairs", ctypes.c_int32), ("slots", ctypes.c_int32)]
+
+
+class RequestInfo(ctypes.Structure):
+    """tal_bsw_request_info: a completed request's status and steady-clock times."""
+    _fields_ = [("status", ctypes.c_int32), ("tick_requests", ctypes.c_int32),
+                ("bad_pair", ctypes.c_int64), ("tick_pairs", ctypes.c_int64),
+                ("submit_ns", ctypes.c_int64), ("admit_ns", ctypes.c_int64),
+                ("launch_ns", ctypes.c_int64), ("done_ns", ctypes.c_int64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("ticks", ctypes.c_uint64), ("pairs", ctypes.c_uint64),
+                ("launches", ctypes.c_uint64), ("pool_bytes", ctypes.c_uint64),
+                ("pool_used_bytes", ctypes.c_uint64), ("pool_peak_bytes", ctypes.c_uint64),
+                ("queued", ctypes.c_int32), ("admitted", ctypes.c_int32), ("running", ctypes.c_int32),
+                ("max_tick_requests", ctypes.c_int32), ("max_ticks_in_flight", ctypes.c_int32),
+                ("pad_", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad_"}
 
 
 def core_lib():
@@ -222,6 +257,95 @@ class BandedPairWiseSW:
         rc = self._lib.tal_bsw_scores(self._h, pa.ctypes.data, _buf_ptr(seqBufRef),
                                       _buf_ptr(seqBufQer), n, int(w), int(bits))
         self._check(rc)
+
+
+def now_ns() -> int:
+    """The serving loop's steady clock, in nanoseconds."""
+    return int(core_lib().tal_bsw_now_ns())
+
+
+class BswServer:
+    """Serving loop over the C ABI (tal_bsw_server_create / tal_bsw_submit /
+    tal_bsw_poll): requests of any size are admitted into a device pool as
+    memory allows and run with continuous batching.  The server keeps a
+    reference to each request's arrays until the request is polled complete
+    (the library reads and writes them until then)."""
+
+    def __init__(self, bsw: BandedPairWiseSW, pool_bytes: int = 0, staging_bytes: int = 0,
+                 max_tick_pairs: int = 0, slots: int = 0):
+        self._lib = core_lib()
+        cfg = ServerConfig(int(pool_bytes), int(staging_bytes), int(max_tick_pairs), int(slots))
+        s = ctypes.c_void_p()
+        rc = self._lib.tal_bsw_server_create(bsw._h, ctypes.byref(cfg), ctypes.byref(s))
+        if rc != TAL_OK:
+            raise TalBswError(rc, "tal_bsw_server_create failed")
+        self._s = s
+        self._keep = {}
+
+    def submit(self, pairArray, seqBufRef, seqBufQer, numPairs: Optional[int] = None, w: int = 100,
+               wpair: Optional[np.ndarray] = None, bits: int = AUTO) -> int:
+        """Queues a request (pairs updated in place when it completes); returns its ticket."""
+        pa = _as_pairs(pairArray) if isinstance(pairArray, np.ndarray) else None
+        if pa is not None:
+            n = pa.shape[0] if numPairs is None else int(numPairs)
+            if n < 0 or n > pa.shape[0]:
+                raise ValueError("numPairs out of range for pairArray")
+            pptr = pa.ctypes.data
+        else:
+            n, pptr = int(numPairs), int(pairArray)
+        wp = None
+        if wpair is not None:
+            if isinstance(wpair, np.ndarray):
+                wpair = np.ascontiguousarray(wpair, np.int32)
+                if wpair.shape[0] < n:
+                    raise ValueError("wpair shorter than numPairs")
+                wp = wpair.ctypes.data
+            else:
+                wp = int(wpair)
+        t = ctypes.c_uint64()
+        rc = self._lib.tal_bsw_submit(self._s, pptr, _buf_ptr(seqBufRef), _buf_ptr(seqBufQer), n,
+                                      int(w), wp, int(bits), ctypes.byref(t))
+        if rc != TAL_OK:
+            raise TalBswError(rc, "tal_bsw_submit refused the request")
+        self._keep[t.value] = (pairArray, seqBufRef, seqBufQer, wpair)
+        return t.value
+
+    def poll(self, ticket: int, timeout_us: int = -1) -> Optional[RequestInfo]:
+        """The request's RequestInfo once complete (the ticket is then
+        released), or None if it is not complete within timeout_us."""
+        info = RequestInfo()
+        rc = self._lib.tal_bsw_poll(self._s, ctypes.c_uint64(ticket), int(timeout_us), ctypes.byref(info))
+        if rc == TAL_ETIMEOUT:
+            return None
+        if rc != TAL_OK:
+            raise TalBswError(rc, "tal_bsw_poll: unknown ticket")
+        self._keep.pop(ticket, None)
+        return info
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        rc = self._lib.tal_bsw_server_get_stats(self._s, ctypes.byref(st))
+        if rc != TAL_OK:
+            raise TalBswError(rc, "tal_bsw_server_get_stats failed")
+        return st.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_s", None):
+            self._lib.tal_bsw_server_destroy(self._s)
+            self._s = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def probe_int_peak(device: int = 0):
