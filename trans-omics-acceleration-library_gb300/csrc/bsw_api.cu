@@ -135,6 +135,7 @@ int tal_bsw_destroy(tal_bsw_handle h) {
         h->bseg.release();
         h->bctrl.release();
         h->btune_seg.release();
+        h->bfork.release();
         for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second.exec);
         h->graphs.clear();
         cudaStreamDestroy(h->stream);

@@ -238,6 +238,23 @@ KConfig bin_kconfig(const tal_bsw_ctx *h, int b, int w) {
     return fit_config(choose_config(w, bin_cols(h, b)), bin_cols(h, b), h->smem_optin);
 }
 
+cudaError_t enqueue_bins_forked(tal_bsw_ctx *h, const SortBufs &sb, const LaunchArgs &base,
+                                const int *count, int n, int w, BinFork &f, cudaStream_t s) {
+    cudaError_t e = cudaEventRecord(f.fork, s);
+    for (int b = kNumBins - 1; b >= 0 && e == cudaSuccess; b--) {
+        const int nb = count ? count[b] : n;
+        if (nb <= 0) continue;
+        e = cudaStreamWaitEvent(f.st[b], f.fork, 0);
+        if (e != cudaSuccess) break;
+        const LaunchArgs A = bin_launch_args(h, sb, base, b, nb, sb.seg + 2 * b);
+        e = launch_config(A, bin_kconfig(h, b, w), h->num_sms, h->smem_optin, f.st[b]);
+        h->launches++;
+        if (e == cudaSuccess) e = cudaEventRecord(f.join[b], f.st[b]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, f.join[b], 0);
+    }
+    return e;
+}
+
 int bin_cols(const tal_bsw_ctx *h, int b) {
     int c = bin_upper(b);
     // the widest one-pair-per-warp configuration must fit the block limit
@@ -252,14 +269,19 @@ namespace {
 cudaError_t enqueue_bins(tal_bsw_ctx *h, DevPair *pairs, const uint8_t *ref, size_t ref_bytes,
                          const uint8_t *qer, size_t qer_bytes, int n, int w, const int32_t *d_w,
                          int bits) {
-    for (int b = 0; b < kNumBins; b++) {
-        LaunchArgs A = bin_args(h, b, pairs, ref, ref_bytes, qer, qer_bytes, n, w, d_w, bits,
-                                reinterpret_cast<const int32_t *>(h->bseg.p) + 2 * b);
-        cudaError_t e = launch_config(A, h->bin_cfg[b], h->num_sms, h->smem_optin, h->stream);
-        if (e != cudaSuccess) return e;
-        h->launches++;
-    }
-    return cudaSuccess;
+    cudaError_t e = h->bfork.create();
+    if (e != cudaSuccess) return e;
+    LaunchArgs base;
+    memset(&base, 0, sizeof(base));
+    base.pairs = pairs;
+    base.ref = ref;
+    base.qer = qer;
+    base.ref_lo = 0; base.ref_hi = (long long)ref_bytes;
+    base.qer_lo = 0; base.qer_hi = (long long)qer_bytes;
+    base.wpair = d_w;
+    base.w = w;
+    base.bits = bits;
+    return enqueue_bins_forked(h, handle_sort_bufs(h), base, nullptr, n, w, h->bfork, h->stream);
 }
 
 // Per bin, times each candidate configuration on up to kSample of the bin's

@@ -68,6 +68,37 @@ struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
 };
 
+// One stream per length bin, forked from and joined back into a caller
+// stream with events, so the bins' launches run side by side: a bin whose
+// last pairs are long no longer holds back the bins after it.
+struct BinFork {
+    cudaStream_t st[kNumBins] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kNumBins] = {};
+    bool ready = false;
+    cudaError_t create() {
+        if (ready) return cudaSuccess;
+        cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+        for (int b = 0; b < kNumBins && e == cudaSuccess; b++) {
+            e = cudaStreamCreateWithFlags(&st[b], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming);
+        }
+        ready = e == cudaSuccess;
+        return e;
+    }
+    void release() {
+        for (int b = 0; b < kNumBins; b++) {
+            if (st[b]) cudaStreamDestroy(st[b]);
+            if (join[b]) cudaEventDestroy(join[b]);
+            st[b] = nullptr;
+            join[b] = nullptr;
+        }
+        if (fork) cudaEventDestroy(fork);
+        fork = nullptr;
+        ready = false;
+    }
+};
+
 // Device buffers of one sort: bucket counts (kNumBuckets), sorted order and
 // -- for a serving tick -- the request of each sorted item, bin segments
 // {offset, count} x kNumBins, control block.
@@ -93,6 +124,11 @@ LaunchArgs bin_launch_args(const tal_bsw_ctx *h, const SortBufs &sb, LaunchArgs 
                            const int32_t *seg);
 cudaError_t enqueue_sort(tal_bsw_ctx *h, const SortBufs &sb, const DevPair *pairs,
                          const ReqDesc *reqs, int nreqs, int n, cudaStream_t s);
+// One launch per bin with count[b] > 0 (all bins when count is NULL), each on
+// its own stream of f, longest queries first, forked from and joined into s.
+// base: the launch's pair source (pairs / windows / bands, or a request table).
+cudaError_t enqueue_bins_forked(tal_bsw_ctx *h, const SortBufs &sb, const LaunchArgs &base,
+                                const int *count, int n, int w, BinFork &f, cudaStream_t s);
 }  // namespace talbsw
 
 struct tal_bsw_ctx {
@@ -105,6 +141,7 @@ struct tal_bsw_ctx {
     talbsw::DevBuf pairs, ref, qer, ctrl, wpair, caps;
     // batched form
     talbsw::DevBuf bcounts, border, bseg, bctrl, btune_seg;
+    talbsw::BinFork bfork;
     bool tuned = false;
     talbsw::KConfig bin_cfg[talbsw::kNumBins];
     std::map<std::tuple<const void *, const void *, size_t, const void *, size_t, int, int,

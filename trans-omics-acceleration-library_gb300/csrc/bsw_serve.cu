@@ -142,6 +142,7 @@ struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     DevBuf counts, order, order_req, seg, ctrl, dreqs;
+    BinFork fork;
     ReqDesc *hreqs = nullptr;  // pinned copy of the tick's request table
     std::vector<Request *> reqs;
     bool busy = false;
@@ -318,14 +319,11 @@ int tal_bsw_server::launch_tick(Slot &sl) {
     sb.seg = reinterpret_cast<int32_t *>(sl.seg.p);
     sb.ctrl = reinterpret_cast<BatchCtrl *>(sl.ctrl.p);
     if (e == cudaSuccess && total > 0) e = enqueue_sort(h, sb, nullptr, dreqs, nreq, (int)total, sl.stream);
-    for (int b = 0; b < kNumBins && e == cudaSuccess; b++) {
-        if (!bins[b]) continue;
-        LaunchArgs A;
-        memset(&A, 0, sizeof(A));
-        A.reqs = dreqs;
-        A = bin_launch_args(h, sb, A, b, bins[b], sb.seg + 2 * b);
-        e = launch_config(A, bin_kconfig(h, b, wmax), h->num_sms, h->smem_optin, sl.stream);
-        h->launches++;
+    if (e == cudaSuccess && total > 0) {
+        LaunchArgs base;
+        memset(&base, 0, sizeof(base));
+        base.reqs = dreqs;
+        e = enqueue_bins_forked(h, sb, base, bins, (int)total, wmax, sl.fork, sl.stream);
     }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(sl.hreqs, dreqs, sizeof(ReqDesc) * nreq, cudaMemcpyDeviceToHost, sl.stream);
@@ -451,6 +449,7 @@ void free_server(tal_bsw_server *s) {
         sl.counts.release(); sl.order.release(); sl.order_req.release();
         sl.seg.release(); sl.ctrl.release(); sl.dreqs.release();
         if (sl.hreqs) cudaFreeHost(sl.hreqs);
+        sl.fork.release();
         if (sl.done) cudaEventDestroy(sl.done);
         if (sl.stream) cudaStreamDestroy(sl.stream);
     }
@@ -526,6 +525,7 @@ int tal_bsw_server_create(tal_bsw_handle src, const tal_bsw_server_config *cfg,
         if (e == cudaSuccess) e = sl.seg.ensure(sizeof(int32_t) * 2 * kNumBins);
         if (e == cudaSuccess) e = sl.ctrl.ensure(sizeof(BatchCtrl));
         if (e == cudaSuccess) e = sl.dreqs.ensure(sizeof(ReqDesc) * kMaxTickRequests);
+        if (e == cudaSuccess) e = sl.fork.create();
         if (e == cudaSuccess)
             e = cudaHostAlloc(reinterpret_cast<void **>(&sl.hreqs), sizeof(ReqDesc) * kMaxTickRequests,
                               cudaHostAllocDefault);
