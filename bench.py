@@ -365,9 +365,11 @@ def run_ours(args):
     batched = {"value": round(total_cells / t_batched / 1e9, 3), "unit": UNIT,
                "pairs_per_s": round(total_pairs / t_batched, 1),
                "ms_per_step": round(t_batched * 1e3, 3),
-               "bins": [list(bsw.bin_config(k)[:2]) for k in range(21)],
-               "note": "device-resident batched call (sort into length bins + per-bin "
-                       "persistent launches, one CUDA graph); wall time per synchronous call"}
+               "segments": [list(bsw.segment_config(k)) for k in range(105)],
+               "note": "device-resident batched call (sort into segments = length bin x band "
+                       "class, one persistent launch per segment on forked streams, one CUDA "
+                       "graph); segments: [lanes per pair, columns per lane, max query, row ring]; "
+                       "wall time per synchronous call"}
 
     # ---- rooflines
     hbm_peak, peak_src = measured_peaks()

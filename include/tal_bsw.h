@@ -120,10 +120,21 @@ int tal_bsw_scores_batched(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t 
  * call tunes again). */
 int tal_bsw_autotune_reset(tal_bsw_handle h);
 
-/* The configuration of length bin `bin` (0..20): lanes per pair (1 = the
- * lane-per-pair kernel), columns per lane, and the bin's largest query length. */
+/* The configuration of length bin `bin` (0..20) for bands too wide for a row
+ * ring: lanes per pair (1 = the lane-per-pair kernel), columns per lane, and
+ * the bin's largest query length. */
 int tal_bsw_bin_config(tal_bsw_handle h, int bin, int *lanes_per_pair, int *cols_per_lane,
                        int *max_len2);
+
+/* The configuration of segment `seg` (0..104) of the batched form.  A
+ * segment is a length bin x band class (class c < 4: pairs with
+ * 2w + 12 <= 64 << c, which the lane kernel scores in a ring of 64 << c
+ * columns; class 4: whole rows); segments 0..10 are the whole-row bins of
+ * queries above 384 columns, longest first, then all other segments, bins
+ * longest first.  max_len2: the bin's largest query; window: the ring in
+ * columns (0: whole rows, or not the lane kernel). */
+int tal_bsw_segment_config(tal_bsw_handle h, int seg, int *lanes_per_pair, int *cols_per_lane,
+                           int *max_len2, int *window);
 
 /* Waits for the handle's stream; returns the first error any launch on it
  * reported since the last sync. */
@@ -203,7 +214,14 @@ typedef struct {
     size_t staging_bytes;   /* pinned host staging for pageable callers; 0 = 1 GiB */
     int32_t max_tick_pairs; /* most pairs in one tick (and in one request);
                                0 = 8,388,608 */
-    int32_t slots;          /* ticks on the device at once, 1..4; 0 = 2 */
+    int32_t slots;          /* ticks on the device at once, 1..4; 0 = 4 */
+    int32_t latency_pairs;  /* ticks with fewer pairs run as a handful of
+                               launches with several lanes per pair above 256
+                               columns (lower latency per pair); larger ticks
+                               run like the batched form, one tuned launch per
+                               segment (more cells per second);
+                               0 = 131,072, -1 = never */
+    int32_t pad_;
 } tal_bsw_server_config;
 
 typedef struct {

@@ -24,8 +24,9 @@ def build(force=False):
     return SO
 
 
-def run(pairs, ref, qer, w, params, bits=16, K=4, warps=1, wpair=None, G=32):
-    """Scores a copy of pairs with the emulated kernel; returns (pairs, err_flags, err_index)."""
+def run(pairs, ref, qer, w, params, bits=16, K=4, warps=1, wpair=None, G=32, win=0):
+    """Scores a copy of pairs with the emulated kernel (win: the lane
+    kernel's row ring, 0 = whole rows); returns (pairs, err_flags, err_index)."""
     global _lib
     if _lib is None:
         _lib = ctypes.CDLL(build())
@@ -43,11 +44,11 @@ def run(pairs, ref, qer, w, params, bits=16, K=4, warps=1, wpair=None, G=32):
                      ctypes.c_longlong(ref.shape[0]), vp(qer.ctypes.data), ctypes.c_longlong(0),
                      ctypes.c_longlong(qer.shape[0]), int(out.shape[0]), int(w),
                      None if wp is None else vp(wp.ctypes.data), int(bits), vp(kp.ctypes.data),
-                     int(G), int(K), int(warps), ctypes.byref(ef), ctypes.byref(ei))
+                     int(G), int(K), int(warps), int(win), ctypes.byref(ef), ctypes.byref(ei))
     return out, ef.value, ei.value
 
 
-def run_reqs(reqs, order, params, K=4, warps=1, G=32):
+def run_reqs(reqs, order, params, K=4, warps=1, G=32, win=0):
     """A serving tick on the emulated kernel.  reqs: list of dicts with
     pairs, ref, qer (the request's byte windows), ref_lo, qer_lo (window
     offsets), w, bits and optional wpair; order: list of (request, local
@@ -79,6 +80,14 @@ def run_reqs(reqs, order, params, K=4, warps=1, G=32):
         P(*[None if x is None else x.ctypes.data for x in wps]),
         I(*[int(x.shape[0]) for x in outs]), I(*[int(r["w"]) for r in reqs]),
         I(*[int(r["bits"]) for r in reqs]), int(o.shape[0]), vp(o.ctypes.data), vp(orq.ctypes.data),
-        vp(kp.ctypes.data), int(G), int(K), int(warps), err, bad)
+        vp(kp.ctypes.data), int(G), int(K), int(warps), int(win), err, bad)
     assert rc == 0, "lanes of a warp exited apart"
     return outs, list(err), list(bad)
+
+
+def window_for(w):
+    """The lane kernel's ring for band w: smallest power of two >= 2w + 12, at least 64."""
+    W = 64
+    while W < 2 * w + 12:
+        W *= 2
+    return W

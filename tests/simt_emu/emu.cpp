@@ -24,7 +24,7 @@ std::mutex atomic_mu;
 // Runs one launch of A (one block of `warps` warps); -1 if a warp's lanes
 // did not finish together (a divergent exit).
 static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps) {
-    size_t wbytes = G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap)
+    size_t wbytes = G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap, A.win)
                            : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G);
     std::vector<unsigned char> smem(wbytes * warps + 64, 0xA5);  // poisoned, like fresh smem
     // warps run one after another; the 32 lanes of a warp are fibers
@@ -83,7 +83,7 @@ static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps) {
 extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long ref_lo,
                            long long ref_hi, const uint8_t *qer, long long qer_lo,
                            long long qer_hi, int n, int w, const int32_t *wpair, int bits,
-                           const int32_t *kp, int G, int K, int warps, int *err_flags,
+                           const int32_t *kp, int G, int K, int warps, int win, int *err_flags,
                            long long *err_index) {
     talbsw::LaunchArgs A;
     std::memset(&A, 0, sizeof(A));
@@ -91,7 +91,7 @@ extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long
     A.ref = ref; A.ref_lo = ref_lo; A.ref_hi = ref_hi;
     A.qer = qer; A.qer_lo = qer_lo; A.qer_hi = qer_hi;
     A.wpair = wpair;
-    A.n = n; A.w = w; A.bits = bits;
+    A.n = n; A.w = w; A.bits = bits; A.win = win;
     int m1 = 1, m2 = 1;
     for (int i = 0; i < n; i++) { m1 = std::max(m1, pairs[i].len1); m2 = std::max(m2, pairs[i].len2); }
     A.cols_cap = m2; A.rows_cap = m1;
@@ -112,7 +112,7 @@ extern "C" int emu_bsw_run_reqs(int nreq, talbsw::DevPair **pairs, const uint8_t
                                 const long long *qer_hi, const int32_t **wpair, const int *n,
                                 const int *w, const int *bits, int nwork, const int32_t *order,
                                 const int32_t *order_req, const int32_t *kp, int G, int K,
-                                int warps, int *req_err, long long *req_bad) {
+                                int warps, int win, int *req_err, long long *req_bad) {
     std::vector<talbsw::ReqDesc> R(nreq);
     int first = 0, m1 = 1, m2 = 1;
     for (int r = 0; r < nreq; r++) {
@@ -134,7 +134,7 @@ extern "C" int emu_bsw_run_reqs(int nreq, talbsw::DevPair **pairs, const uint8_t
     A.order = order;
     A.order_req = order_req;
     A.n = nwork;
-    A.cols_cap = m2; A.rows_cap = m1;
+    A.cols_cap = m2; A.rows_cap = m1; A.win = win;
     int counter = 0, flags = 0;
     long long bad = (long long)INT64_MAX;
     A.work_counter = &counter; A.err_flags = &flags; A.err_index = &bad;

@@ -112,7 +112,7 @@ def test_serving_admission_waits_for_pool_memory(c3):
     arrival order and all complete; one larger than the pool is refused."""
     wl, b, P, exp = c3
     pool = 4 << 20
-    with _bsw(P) as bsw, tal_bsw.BswServer(bsw, pool_bytes=pool) as srv:
+    with _bsw(P) as bsw, tal_bsw.BswServer(bsw, pool_bytes=pool, latency_pairs=-1) as srv:
         got = b.pairs.copy()
         spans = [(lo, lo + 4000) for lo in range(0, 48000, 4000)]   # ~1.5 MB each
         tickets = [srv.submit(got[lo:hi], b.ref, b.qer, w=100, wpair=b.w[lo:hi], bits=0)

@@ -45,9 +45,11 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
     A.err_index = &c->bad_index;
     A.cells = &c->cells;
     A.P = h->kp;
-    const talbsw::KConfig cfg =
-        talbsw::fit_config(talbsw::choose_config(w_for_k, A.cols_cap), A.cols_cap, h->smem_optin);
-    if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap) > h->smem_optin)
+    // one band for every pair: the lane kernel keeps a ring of columns
+    A.win = A.wpair ? 0 : talbsw::lane_window(A.w, A.cols_cap);
+    const talbsw::KConfig cfg = talbsw::fit_config(talbsw::choose_config(w_for_k, A.cols_cap, A.win),
+                                                   A.cols_cap, h->smem_optin, A.win);
+    if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap, A.win) > h->smem_optin)
         return fail(h, TAL_EDOMAIN, "pair too long for the shared-memory row buffers");
     Ctrl init = {0, 0, (long long)INT64_MAX, 0ull};
     cudaError_t e = cudaMemcpyAsync(c, &init, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream);

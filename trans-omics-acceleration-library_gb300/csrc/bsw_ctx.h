@@ -52,13 +52,60 @@ __host__ __device__ constexpr int bin_upper(int b) {
         default: return 32767;
     }
 }
-constexpr int kRowBuckets = 4096;  // len1 / 8, capped
-constexpr int kNumBuckets = kNumBins * kRowBuckets;
+// Band classes within a length bin: class c < 4 holds pairs whose band fits
+// a ring of 64 << c columns (2w + 12 <= 64 << c) in the lane kernel; class 4
+// holds whole rows.  A class whose ring would be no smaller than the bin's
+// whole rows folds into class 4.  A segment is a (length bin, band class).
+constexpr int kNumCls = 5;
+__host__ __device__ inline int seg_cls(int b, long long w) {
+    for (int c = 0; c < kNumCls - 1; c++) {
+        const long long W = 64LL << c;
+        if (W >= bin_upper(b) + 4) return kNumCls - 1;
+        if (2 * w + 12 <= W) return c;
+    }
+    return kNumCls - 1;
+}
 
-// Control block on the device for one call: work counters (one per bin),
-// error flags, first bad pair, cell count.
+// Segment order of the sort (positions 0..kNumSegs-1): first the whole-row
+// segments of queries above 384 columns (too wide for the lane kernel),
+// bins longest first; then every other segment, bins longest first, classes
+// in order.  Each bin's segments are consecutive there, and so is any run of
+// bins from bin 0 up, so a launch can take one bin, or all bins up to a
+// length, as one range.
+constexpr int kRowSegs = 11;                  // positions 0..10: bins 20..10, class 4
+constexpr int kNumSegs = kRowSegs + 44 + 50;  // bins 20..10: classes 0-3; bins 9..0: classes 0-4
+__host__ __device__ inline int seg_index(int b, int c) {
+    if (c == kNumCls - 1 && b >= 10) return 20 - b;
+    return kRowSegs + (b >= 10 ? (20 - b) * 4 : 44 + (9 - b) * 5) + c;
+}
+__host__ __device__ inline int seg_bin(int s) {
+    if (s < kRowSegs) return 20 - s;
+    const int r = s - kRowSegs;
+    return r < 44 ? 20 - r / 4 : 9 - (r - 44) / 5;
+}
+__host__ __device__ inline int seg_class(int s) {
+    if (s < kRowSegs) return kNumCls - 1;
+    const int r = s - kRowSegs;
+    return r < 44 ? r % 4 : (r - 44) % 5;
+}
+// First and last position of bin b's ring / lane segments (not its
+// whole-row segment when b >= 10).
+__host__ __device__ inline int seg_first(int b) { return seg_index(b, 0); }
+__host__ __device__ inline int seg_last(int b) { return seg_index(b, b >= 10 ? kNumCls - 2 : kNumCls - 1); }
+// The lane kernel's ring for segment s: 64 << c for class c < 4, 0 (whole
+// rows) for class 4.
+__host__ __device__ inline int seg_window(int s) {
+    const int c = seg_class(s);
+    return c < kNumCls - 1 ? (64 << c) : 0;
+}
+
+constexpr int kRowBuckets = 512;  // len1 / 8, capped
+constexpr int kNumBuckets = kNumSegs * kRowBuckets;
+
+// Control block on the device for one call: work counters (one per
+// segment), error flags, first bad pair, cell count.
 struct BatchCtrl {
-    int counter[kNumBins + 1];
+    int counter[kNumSegs + 1];
     int flags;
     long long bad_index;
     unsigned long long cells;
@@ -68,18 +115,20 @@ struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
 };
 
-// One stream per length bin, forked from and joined back into a caller
-// stream with events, so the bins' launches run side by side: a bin whose
-// last pairs are long no longer holds back the bins after it.
+// Streams forked from and joined back into a caller stream with events, so
+// the segments' launches run side by side: a segment whose last pairs are
+// long no longer holds back the ones after it.  Segment s runs on stream
+// s % kForkStreams.
+constexpr int kForkStreams = 32;
 struct BinFork {
-    cudaStream_t st[kNumBins] = {};
+    cudaStream_t st[kForkStreams] = {};
     cudaEvent_t fork = nullptr;
-    cudaEvent_t join[kNumBins] = {};
+    cudaEvent_t join[kForkStreams] = {};
     bool ready = false;
     cudaError_t create() {
         if (ready) return cudaSuccess;
         cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
-        for (int b = 0; b < kNumBins && e == cudaSuccess; b++) {
+        for (int b = 0; b < kForkStreams && e == cudaSuccess; b++) {
             e = cudaStreamCreateWithFlags(&st[b], cudaStreamNonBlocking);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming);
         }
@@ -87,7 +136,7 @@ struct BinFork {
         return e;
     }
     void release() {
-        for (int b = 0; b < kNumBins; b++) {
+        for (int b = 0; b < kForkStreams; b++) {
             if (st[b]) cudaStreamDestroy(st[b]);
             if (join[b]) cudaEventDestroy(join[b]);
             st[b] = nullptr;
@@ -100,8 +149,8 @@ struct BinFork {
 };
 
 // Device buffers of one sort: bucket counts (kNumBuckets), sorted order and
-// -- for a serving tick -- the request of each sorted item, bin segments
-// {offset, count} x kNumBins, control block.
+// -- for a serving tick -- the request of each sorted item, segments
+// {offset, count} x kNumSegs, control block.
 struct SortBufs {
     int *counts;
     int32_t *order;
@@ -117,18 +166,26 @@ struct tal_bsw_ctx;
 namespace talbsw {
 // Implemented in bsw_batched.cu; used by the serving loop (bsw_serve.cu).
 int bin_cols(const tal_bsw_ctx *h, int b);
-// Kernel and tile of length bin b: the autotuner's choice, else the default
+// Kernel and tile of segment seg: the autotuner's choice, else the default
 // for band w.
-KConfig bin_kconfig(const tal_bsw_ctx *h, int b, int w);
-LaunchArgs bin_launch_args(const tal_bsw_ctx *h, const SortBufs &sb, LaunchArgs A, int b, int n,
-                           const int32_t *seg);
-cudaError_t enqueue_sort(tal_bsw_ctx *h, const SortBufs &sb, const DevPair *pairs,
-                         const ReqDesc *reqs, int nreqs, int n, cudaStream_t s);
-// One launch per bin with count[b] > 0 (all bins when count is NULL), each on
-// its own stream of f, longest queries first, forked from and joined into s.
-// base: the launch's pair source (pairs / windows / bands, or a request table).
-cudaError_t enqueue_bins_forked(tal_bsw_ctx *h, const SortBufs &sb, const LaunchArgs &base,
-                                const int *count, int n, int w, BinFork &f, cudaStream_t s);
+KConfig seg_kconfig(const tal_bsw_ctx *h, int seg, int w);
+LaunchArgs seg_launch_args(const tal_bsw_ctx *h, const SortBufs &sb, LaunchArgs A, int seg, int n);
+// Sorts the pairs into (segment, target-length bucket) order.  The pairs are
+// base's (pairs, bands wpair / w) or, when base.reqs is set, the
+// concatenation of the nreqs requests of that table.
+cudaError_t enqueue_sort(tal_bsw_ctx *h, const SortBufs &sb, const LaunchArgs &base, int nreqs,
+                         int n, cudaStream_t s);
+// A serving tick's launches (count: pairs per segment, known on the host):
+// bins above lane_bin with G lanes per pair, bins 0..lane_bin in one
+// lane-kernel launch.
+cudaError_t enqueue_tick(tal_bsw_ctx *h, const SortBufs &sb, const LaunchArgs &base,
+                         const int *count, int lane_bin, BinFork &f, cudaStream_t s);
+// One launch per segment with count[seg] > 0 (all when count is NULL),
+// longest queries first, on streams of f forked from and joined into s;
+// latency: per-pair latency configurations instead of the tuned ones.
+cudaError_t enqueue_segs_forked(tal_bsw_ctx *h, const SortBufs &sb, const LaunchArgs &base,
+                                const int *count, int n, int w, BinFork &f, cudaStream_t s,
+                                bool latency);
 }  // namespace talbsw
 
 struct tal_bsw_ctx {
@@ -143,7 +200,7 @@ struct tal_bsw_ctx {
     talbsw::DevBuf bcounts, border, bseg, bctrl, btune_seg;
     talbsw::BinFork bfork;
     bool tuned = false;
-    talbsw::KConfig bin_cfg[talbsw::kNumBins];
+    talbsw::KConfig bin_cfg[talbsw::kNumSegs];
     std::map<std::tuple<const void *, const void *, size_t, const void *, size_t, int, int,
                         const void *, int>, talbsw::GraphEntry> graphs;
     std::mutex mu;

@@ -84,12 +84,14 @@ struct LaunchArgs {
     const uint8_t *qer;
     long long ref_lo, ref_hi, qer_lo, qer_hi;
     const int32_t *order;    // optional permutation (batched form)
-    const int32_t *seg;      // optional {offset, count} into order (overrides n)
+    const int32_t *seg;      // optional {offset, count} pairs into order (overrides n):
+    int nseg;                // the launch takes the nseg (>= 1) consecutive segments there
     const int32_t *wpair;    // optional per-pair band
     int32_t n;
     int32_t w;
     int bits;                // 8, 16 or 0 = per-pair routing
     int cols_cap, rows_cap;  // shared-memory row capacity per pair
+    int win;                 // lane kernel: ring of win columns per pair (0: whole rows)
     int *work_counter;       // next work item (dynamic scheduling)
     unsigned long long *cells;  // optional: total DP cells computed
     int *err_flags;
@@ -129,6 +131,14 @@ __device__ __forceinline__ PairSrc pair_src(const LaunchArgs &A, int pidx, int r
         s.bits = A.bits;
     }
     return s;
+}
+
+// Work items of a launch: the consecutive segments seg[0 .. nseg) of the
+// sorted order, or items 0..n of the launch's pairs.
+__device__ __forceinline__ int work_count(const LaunchArgs &A) {
+    if (!A.seg) return A.n;
+    const int last = A.nseg > 1 ? A.nseg - 1 : 0;
+    return A.seg[2 * last] + A.seg[2 * last + 1] - A.seg[0];
 }
 
 // Records an error for pair pidx (of request req, or of the launch).
@@ -522,7 +532,7 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
     PairState ps;
     ps.pidx = 0; ps.req = -1; ps.pp = nullptr; ps.nrow = 0; ps.ncol = 0; ps.i = 0; ps.ncells = 0;
     bool active = false, done = false;
-    const int nwork = A.seg ? A.seg[1] : A.n;
+    const int nwork = work_count(A);
     const int32_t *order = A.seg ? A.order + A.seg[0] : A.order;
     const int32_t *order_req = A.reqs ? (A.seg ? A.order_req + A.seg[0] : A.order_req) : nullptr;
 

@@ -17,6 +17,17 @@
 //                      columns' scores in the row's score table at once
 // The target base of each row is read from global memory (one byte per row).
 //
+// Windowed rows: a row of the reference touches only columns
+// [i - w, i + w + 3] (band, its last column, the lazily initialised columns
+// ahead of it), so HF and QS may be rings of W >= 2w + 12 columns (a power of
+// two; column j lives in slot j & (W - 1)) instead of whole rows, which
+// makes the shared memory per pair depend on the band, not on the query
+// length.  The one read of the reference below the band -- the 16-bit head
+// re-derivation scans from nbeg, which may lag behind the band, over columns
+// that left the band rows ago -- is answered from `p`, the first nonzero of
+// those frozen columns, recorded as each column leaves the band (a column
+// left of the band is never written again).
+//
 // The inner loop over a row's band is split into the columns left of the
 // per-pair head (masked), the clean middle, and the columns at/after the tail,
 // so the middle -- nearly every cell -- runs without predicates.
@@ -26,14 +37,27 @@
 
 namespace talbsw {
 
-__host__ __device__ __forceinline__ size_t lane_hf_words(int cols_cap) {
-    return (size_t)(cols_cap + 4) * 32;
+// win = 0: whole rows of cols_cap + 4 columns; else a ring of win columns.
+__host__ __device__ __forceinline__ size_t lane_hf_words(int cols_cap, int win) {
+    return (size_t)(win > 0 ? win : cols_cap + 4) * 32;
 }
-__host__ __device__ __forceinline__ size_t lane_qs_words(int cols_cap) {
-    return (size_t)((cols_cap + 7) / 8 + 2) * 32;
+__host__ __device__ __forceinline__ size_t lane_qs_words(int cols_cap, int win) {
+    return (size_t)(win > 0 ? win / 8 : (cols_cap + 7) / 8 + 2) * 32;
 }
-__host__ __device__ __forceinline__ size_t lane_warp_smem_bytes(int cols_cap) {
-    return (lane_hf_words(cols_cap) + lane_qs_words(cols_cap)) * 4;
+__host__ __device__ __forceinline__ size_t lane_warp_smem_bytes(int cols_cap, int win) {
+    return (lane_hf_words(cols_cap, win) + lane_qs_words(cols_cap, win)) * 4;
+}
+
+// Smallest ring (a power of two, at least 64 columns) of at least `cols`.
+__host__ __device__ __forceinline__ int lane_ring_at_least(long long cols) {
+    int W = 64;
+    while (W < (1 << 30) && (long long)W < cols) W <<= 1;
+    return W;
+}
+
+// Smallest ring that holds every column a row with band w touches.
+__host__ __device__ __forceinline__ int lane_window_for(long long w) {
+    return lane_ring_at_least(2 * w + 12);
 }
 
 // Score of query code q (0..4) against the row's table, sign-extended.
@@ -105,6 +129,7 @@ struct LanePair {
     DevPair *pp;
     const uint8_t *q, *t;
     int pidx, req;
+    int fend, p;   // frozen columns [nbeg, fend) seen; p: first nonzero of them, or -1
     int nrow, ncol, i, initc, tnext;
     int head, tail, nbeg, nend;
     int maxScore, x, y, gscore, max_off, max_ie;
@@ -122,16 +147,20 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     uint32_t *wsm = reinterpret_cast<uint32_t *>(smem_raw) +
-                    (size_t)wib * (lane_hf_words(A.cols_cap) + lane_qs_words(A.cols_cap));
-    uint32_t *HF = wsm + lane;                              // HF[j * 32]
-    uint32_t *QS = wsm + lane_hf_words(A.cols_cap) + lane;  // QS[(j / 8) * 32]
+                    (size_t)wib * (lane_hf_words(A.cols_cap, A.win) + lane_qs_words(A.cols_cap, A.win));
+    uint32_t *HF = wsm + lane;                                     // column j: HF[slot(j) * 32]
+    uint32_t *QS = wsm + lane_hf_words(A.cols_cap, A.win) + lane;  // columns 8q..8q+7: QS[qslot(q) * 32]
+    const int wm = A.win > 0 ? A.win - 1 : -1;  // column -> slot mask (-1: whole rows)
+    const int qm = wm >> 3;                     // query word -> slot mask
+    auto hf = [&](int j) -> uint32_t & { return HF[(uint32_t)(j & wm) << 5]; };
+    auto qs = [&](int j) -> uint32_t & { return QS[(uint32_t)((j >> 3) & qm) << 5]; };
     const KernelParams P = A.P;
     const int oe_ins = P.o_ins + P.e_ins, oe_del = P.o_del + P.e_del;
     const int e_ins = P.e_ins, e_del = P.e_del;
 
     LanePair s = {};
     bool active = false;
-    const int nwork = A.seg ? A.seg[1] : A.n;
+    const int nwork = work_count(A);
     const int32_t *order = A.seg ? A.order + A.seg[0] : A.order;
     const int32_t *order_req = A.reqs ? (A.seg ? A.order_req + A.seg[0] : A.order_req) : nullptr;
     auto fail = [&](int flag, int req, int pidx) { report_error(A, req, flag, pidx); };
@@ -168,7 +197,10 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                             (long long)idr >= src.ref_lo && (long long)idq >= src.qer_lo &&
                             (long long)idr + len1 <= src.ref_hi && (long long)idq + len2 <= src.qer_hi;
             if (!ok) { fail(ERR_DOMAIN, req, pidx); continue; }
-            if (len2 > A.cols_cap) { fail(ERR_CAPACITY, req, pidx); continue; }
+            if (A.win > 0 ? (2LL * wcall + 12 > A.win && len2 + 4 > A.win) : (len2 > A.cols_cap)) {
+                fail(ERR_CAPACITY, req, pidx);
+                continue;
+            }
             // per-pair constants (smithWatermanBatchWrapper16/8 set-up)
             s.pp = pp;
             s.pidx = pidx;
@@ -209,6 +241,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             s.head = 0; s.tail = s.qlenE;
             s.maxScore = s.h0e; s.x = 0; s.y = 0; s.gscore = -1; s.max_off = 0; s.max_ie = 0;
             s.nbeg = 0; s.nend = len2;
+            s.fend = 0; s.p = -1;
             s.tnext = len1 > 0 ? s.t[0] : 0;
             active = true;
         }
@@ -231,7 +264,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                 else if (k == 1) hv = s.v1;
                 else if (k < ncol) hv = imax(s.v1 - (k - 1) * e_ins, 0);
                 else hv = 0;
-                HF[k * 32] = (uint32_t)hv;
+                hf(k) = (uint32_t)hv;
                 if (!(k & 7) && k < ncol) {
                     uint32_t wq = 0;
                     const int m = imin(8, ncol - k);
@@ -240,7 +273,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                         bad |= c > 4u;
                         wq |= (c & 7u) << (4 * b);
                     }
-                    QS[(k >> 3) * 32] = wq;
+                    qs(k) = wq;
                 }
             }
             if (lim + 1 > s.initc) s.initc = lim + 1;
@@ -250,6 +283,14 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         if (beg < i - s.wk) beg = i - s.wk;
         if (end > i + s.wk + 1) end = i + s.wk + 1;
         if (end > ncol) end = ncol;
+        // columns that left the band since the last row are frozen: note the
+        // first nonzero one at or after nbeg (16-bit head re-derivation)
+        if (!s.is8) {
+            if (s.p < 0)
+                for (int c = imax(s.fend, s.nbeg); c < beg; c++)
+                    if (hf(c) != 0u) { s.p = c; break; }
+            s.fend = imax(s.fend, beg);
+        }
         int h10init = 0;  // H_v[i+1] (:3065-3067)
         if (beg == 0) {
             const int k = i + 1;
@@ -268,7 +309,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         s.tail = tail;
         if (head != phead || tail != ptail) {
             const int hi = imin(end, head);
-            for (int l = beg; l < hi; l++) HF[l * 32] = 0u;
+            for (int l = beg; l < hi; l++) hf(l) = 0u;
         }
         // row exit status (:3119-3129); outputs freeze once a pair exits
         if (i1 > s.mlen || tail == head || head > tail) { finish(); continue; }
@@ -295,21 +336,21 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         const int jB = imax(imin(end, tail), jA);   // columns j >= tail: not in the max
         if (end > beg) s.ncells += (unsigned long long)(end - beg);
         for (int j = beg; j < jA; j++) {
-            const uint32_t w = HF[j * 32];
-            const uint32_t q = (QS[(j >> 3) * 32] >> (4 * (j & 7))) & 0xfu;
+            const uint32_t w = hf(j);
+            const uint32_t q = (qs(j) >> (4 * (j & 7))) & 0xfu;
             int f2;
             hprev = lane_cell(w, lane_score1(tlo, thi, q), e, f2, oe_ins, e_ins, oe_del, e_del);
-            HF[j * 32] = 0u;  // masked: H and F stored as zero
+            hf(j) = 0u;  // masked: H and F stored as zero
         }
         {
             int j = jA;
             // single columns up to a multiple of 4
             for (; (j & 3) && j < jB; j++) {
-                const uint32_t w = HF[j * 32];
-                const uint32_t q = (QS[(j >> 3) * 32] >> (4 * (j & 7))) & 0xfu;
+                const uint32_t w = hf(j);
+                const uint32_t q = (qs(j) >> (4 * (j & 7))) & 0xfu;
                 int f2;
                 const int H = lane_cell(w, lane_score1(tlo, thi, q), e, f2, oe_ins, e_ins, oe_del, e_del);
-                HF[j * 32] = __byte_perm((uint32_t)hprev, (uint32_t)f2, 0x5410u);
+                hf(j) = __byte_perm((uint32_t)hprev, (uint32_t)f2, 0x5410u);
                 const uint32_t kk = __byte_perm((uint32_t)(j + 1), (uint32_t)H, 0x5410u);
                 key = kk > key ? kk : key;
                 hprev = H;
@@ -318,20 +359,21 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             if constexpr ((V & 1) == 0) {
                 // next group's row words loaded before this group is computed
                 if (j + 3 < jB) {
-                    uint32_t w0 = HF[j * 32], w1 = HF[(j + 1) * 32], w2 = HF[(j + 2) * 32],
-                             w3 = HF[(j + 3) * 32];
-                    uint32_t qw = QS[(j >> 3) * 32] >> (4 * (j & 4));
+                    uint32_t *hp = &hf(j);
+                    uint32_t w0 = hp[0], w1 = hp[32], w2 = hp[64], w3 = hp[96];
+                    uint32_t qw = qs(j) >> (4 * (j & 4));
                     for (;;) {
                         const int jn = j + 4;
                         const bool more = jn + 3 < jB;
                         uint32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0, nq = 0;
+                        uint32_t *hn = &hf(jn);
                         if (more) {
-                            n0 = HF[jn * 32]; n1 = HF[(jn + 1) * 32];
-                            n2 = HF[(jn + 2) * 32]; n3 = HF[(jn + 3) * 32];
-                            nq = QS[(jn >> 3) * 32] >> (4 * (jn & 4));
+                            n0 = hn[0]; n1 = hn[32]; n2 = hn[64]; n3 = hn[96];
+                            nq = qs(jn) >> (4 * (jn & 4));
                         }
-                        lane_group4<SYM>(HF + j * 32, j, w0, w1, w2, w3, qw, tlo, thi, e, hprev, key,
+                        lane_group4<SYM>(hp, j, w0, w1, w2, w3, qw, tlo, thi, e, hprev, key,
                                          oe_ins, e_ins, oe_del, e_del);
+                        hp = hn;
                         j = jn;
                         if (!more) break;
                         w0 = n0; w1 = n1; w2 = n2; w3 = n3; qw = nq;
@@ -340,32 +382,32 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             } else {
                 // plain loop over groups; two groups per iteration so that
                 // the second group's loads can be issued early
-                uint32_t *hp = HF + j * 32;
 #pragma unroll 2
-                for (; j + 3 < jB; j += 4, hp += 128) {
-                    const uint32_t qw = QS[(j >> 3) * 32] >> (4 * (j & 4));
+                for (; j + 3 < jB; j += 4) {
+                    uint32_t *hp = &hf(j);
+                    const uint32_t qw = qs(j) >> (4 * (j & 4));
                     lane_group4<SYM>(hp, j, hp[0], hp[32], hp[64], hp[96], qw, tlo, thi, e, hprev,
                                      key, oe_ins, e_ins, oe_del, e_del);
                 }
             }
             for (; j < jB; j++) {
-                const uint32_t w = HF[j * 32];
-                const uint32_t q = (QS[(j >> 3) * 32] >> (4 * (j & 7))) & 0xfu;
+                const uint32_t w = hf(j);
+                const uint32_t q = (qs(j) >> (4 * (j & 7))) & 0xfu;
                 int f2;
                 const int H = lane_cell(w, lane_score1(tlo, thi, q), e, f2, oe_ins, e_ins, oe_del, e_del);
-                HF[j * 32] = __byte_perm((uint32_t)hprev, (uint32_t)f2, 0x5410u);
+                hf(j) = __byte_perm((uint32_t)hprev, (uint32_t)f2, 0x5410u);
                 const uint32_t kk = __byte_perm((uint32_t)(j + 1), (uint32_t)H, 0x5410u);
                 key = kk > key ? kk : key;
                 hprev = H;
             }
         }
         for (int j = jB; j < end; j++) {
-            const uint32_t w = HF[j * 32];
-            const uint32_t q = (QS[(j >> 3) * 32] >> (4 * (j & 7))) & 0xfu;
+            const uint32_t w = hf(j);
+            const uint32_t q = (qs(j) >> (4 * (j & 7))) & 0xfu;
             int f2;
             const int H = lane_cell(w, lane_score1(tlo, thi, q), e, f2, oe_ins, e_ins, oe_del, e_del);
             // j >= tail: not in the row maximum; j > tail: H and F stored as zero
-            HF[j * 32] = (j > tail) ? 0u : __byte_perm((uint32_t)hprev, (uint32_t)f2, 0x5410u);
+            hf(j) = (j > tail) ? 0u : __byte_perm((uint32_t)hprev, (uint32_t)f2, 0x5410u);
             hprev = H;
         }
         // last column of the row (:3197-3203)
@@ -373,7 +415,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         {
             const int jl = ran ? end : beg;
             const bool m = (head > jl) || (jl > tail);
-            if (jl <= ncol + 1) HF[jl * 32] = m ? 0u : ((uint32_t)hprev & 0xffffu);
+            if (jl <= ncol + 1) hf(jl) = m ? 0u : ((uint32_t)hprev & 0xffffu);
         }
         // gscore at the query's last column (:3177-3195): in the band exactly
         // when end == ncol, and then it is column end-1
@@ -404,10 +446,14 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         }
         {   // band narrowing (:3235-3260)
             int l = beg;
-            while (l < end && HF[l * 32] == 0u) l++;
-            if (l > beg) s.nbeg = l - 1;
+            while (l < end && hf(l) == 0u) l++;
+            if (l > beg) {  // nbeg >= beg: no frozen columns at or after it yet
+                s.nbeg = l - 1;
+                s.fend = s.nbeg;
+                s.p = -1;
+            }
             l = end;
-            while (l >= beg && HF[l * 32] == 0u) l--;
+            while (l >= beg && hf(l) == 0u) l--;
             s.nend = (l + 2 < ncol) ? l + 2 : ncol;
         }
         {   // per-pair head / tail (:3265-3316; 8-bit: the row's own range :2571-2621)
@@ -415,13 +461,25 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             const int E = s.is8 ? end : s.nend;
             if (E > B) {
                 int l = B;
-                while (l < E && HF[l * 32] == 0u) l++;
+                bool found = false;
+                if (l < beg) {  // frozen columns [nbeg, beg): their first nonzero
+                    if (s.p >= 0 && s.p < E) { l = s.p; found = true; }
+                    else l = imin(beg, E);
+                }
+                if (!found) while (l < E && hf(l) == 0u) l++;
                 if (l > B) s.head = wrapS(l, sh);
             }
             int index = s.tail;
             if (E >= B) {
+                // a cell with H > 0 left a nonzero in [beg + 1, end], so this
+                // scan stops inside the band
                 int l = E;
-                while (l >= B && HF[l * 32] == 0u) l--;
+                while (l >= B && hf(l) == 0u) l--;
+                if (l < beg && wm >= 0) {  // would have read a ring slot reused since
+                    fail(ERR_CAPACITY, s.req, s.pidx);
+                    active = false;
+                    continue;
+                }
                 if (l != E) index = l;
             }
             index = wrapS(index + 2, sh);

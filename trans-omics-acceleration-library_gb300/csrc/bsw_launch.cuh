@@ -6,6 +6,9 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "bsw_kernel.cuh"
 #include "bsw_lane.cuh"
@@ -23,11 +26,19 @@ struct KConfig {
 // row is not a long serial walk.  TAL_BSW_G / TAL_BSW_K override (tuning).
 constexpr int kLaneMaxCols = 384;
 
-inline KConfig choose_config(int w, int cols_cap) {
+// Ring size for a launch whose pairs all have band <= w and query length
+// <= cols_cap: 0 (whole rows) unless a ring is smaller.
+inline int lane_window(long long w, int cols_cap) {
+    if (w < 0) return 0;
+    const int W = lane_window_for(w);
+    return W < cols_cap + 4 ? W : 0;
+}
+
+inline KConfig choose_config(int w, int cols_cap, int win = 0) {
     long long bw = std::min<long long>(2LL * std::max(w, 0) + 1, (long long)cols_cap);
     KConfig c;
     c.K = 4;
-    if (cols_cap <= kLaneMaxCols) c.G = 1;
+    if ((win > 0 ? win - 4 : cols_cap) <= kLaneMaxCols) c.G = 1;
     else if (bw <= 64) c.G = 4;
     else if (bw <= 256) c.G = 8;
     else if (bw <= 640) c.G = 16;
@@ -43,6 +54,35 @@ inline KConfig choose_config(int w, int cols_cap) {
     return c;
 }
 
+// Resident blocks per SM of kernel kern at (threads, smem) on the current
+// device.  The shared-memory opt-in is raised to the device limit once per
+// kernel and device, and the occupancy is cached: both queries cost
+// microseconds, and a serving tick issues dozens of launches.
+inline cudaError_t resident_blocks(const void *kern, int threads, size_t smem, size_t smem_optin,
+                                   int *bps) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void *, int, int, size_t>, int> occ;
+    static std::map<std::pair<const void *, int>, bool> raised;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_tuple(kern, dev, threads, smem);
+    auto it = occ.find(key);
+    if (it != occ.end()) {
+        *bps = it->second;
+        return cudaSuccess;
+    }
+    if (!raised[std::make_pair(kern, dev)]) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin);
+        if (e != cudaSuccess) return e;
+        raised[std::make_pair(kern, dev)] = true;
+    }
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, kern, threads, smem);
+    if (e == cudaSuccess) occ[key] = *bps;
+    return e;
+}
+
 template <int G, int K>
 inline cudaError_t launch_gk(const LaunchArgs &A, int num_sms, size_t smem_optin, cudaStream_t s) {
     auto kern = bsw_kernel<G, K>;
@@ -51,10 +91,8 @@ inline cudaError_t launch_gk(const LaunchArgs &A, int num_sms, size_t smem_optin
     while (wpb > 1 && (size_t)wpb * wbytes * 2 > smem_optin) wpb >>= 1;
     const size_t smem = (size_t)wpb * wbytes;
     if (smem > smem_optin) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     int bps = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, smem);
+    cudaError_t e = resident_blocks((const void *)kern, 32 * wpb, smem, smem_optin, &bps);
     if (e != cudaSuccess) return e;
     if (bps < 1) return cudaErrorInvalidConfiguration;
     long long blocks = (long long)bps * num_sms;
@@ -72,15 +110,13 @@ inline cudaError_t launch_lane(const LaunchArgs &A, int num_sms, size_t smem_opt
     if (!sym) v &= 1;
     auto kern = v == 0 ? bsw_lane_kernel<0> : v == 1 ? bsw_lane_kernel<1>
               : v == 2 ? bsw_lane_kernel<2> : bsw_lane_kernel<3>;
-    const size_t wbytes = lane_warp_smem_bytes(A.cols_cap);
+    const size_t wbytes = lane_warp_smem_bytes(A.cols_cap, A.win);
     int wpb = 4;
     while (wpb > 1 && (size_t)wpb * wbytes > 48 * 1024) wpb >>= 1;
     const size_t smem = (size_t)wpb * wbytes;
     if (smem > smem_optin) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     int bps = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * wpb, smem);
+    cudaError_t e = resident_blocks((const void *)kern, 32 * wpb, smem, smem_optin, &bps);
     if (e != cudaSuccess) return e;
     if (bps < 1) return cudaErrorInvalidConfiguration;
     long long blocks = (long long)bps * num_sms;
@@ -90,16 +126,31 @@ inline cudaError_t launch_lane(const LaunchArgs &A, int num_sms, size_t smem_opt
     return cudaGetLastError();
 }
 
+// Lowest-latency configuration for queries up to cols_cap columns: one lane
+// walks a whole pair in the lane kernel, so a pair of many hundred columns
+// holds its warp for milliseconds; G lanes per pair split each row.  Used
+// when a launch is too small to fill the GPU, where the slowest pair, not the
+// cells per second, sets the time.
+constexpr int kLongQuery = 768;  // queries above this always run with G lanes per pair in ticks
+
+inline KConfig latency_config(int cols_cap, int win) {
+    if (cols_cap <= 256) return choose_config(0, cols_cap, win);
+    KConfig c;
+    c.K = 4;
+    c.G = cols_cap <= 512 ? 8 : cols_cap <= 1024 ? 16 : 32;
+    return c;
+}
+
 // Shared memory one warp of the chosen configuration needs.
-inline size_t config_smem(const KConfig &c, int cols_cap, int rows_cap) {
-    if (c.G == 1) return lane_warp_smem_bytes(cols_cap);
+inline size_t config_smem(const KConfig &c, int cols_cap, int rows_cap, int win = 0) {
+    if (c.G == 1) return lane_warp_smem_bytes(cols_cap, win);
     return warp_smem_bytes(cols_cap, rows_cap, c.G);
 }
 
 // Widens the lanes per pair (fewer pairs per warp, less shared memory per
 // warp) until one warp's rows fit a block.
-inline KConfig fit_config(KConfig c, int cols_cap, size_t smem_optin) {
-    while (c.G < 32 && config_smem(c, cols_cap, 1) > smem_optin) c.G = c.G == 1 ? 4 : c.G * 2;
+inline KConfig fit_config(KConfig c, int cols_cap, size_t smem_optin, int win = 0) {
+    while (c.G < 32 && config_smem(c, cols_cap, 1, win) > smem_optin) c.G = c.G == 1 ? 4 : c.G * 2;
     return c;
 }
 

@@ -146,9 +146,10 @@ extern "C" int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_s
     A.err_index = &c->bad_index;
     A.cells = &c->cells;
     A.P = {p.o_del, p.e_del, p.o_ins, p.e_ins, p.zdrop, p.end_bonus, p.w_match, p.w_mismatch};
-    const talbsw::KConfig cfg =
-        talbsw::fit_config(talbsw::choose_config(w, A.cols_cap), A.cols_cap, g_smem_optin[dev]);
-    if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap) > g_smem_optin[dev])
+    A.win = d_w ? 0 : talbsw::lane_window(w, A.cols_cap);
+    const talbsw::KConfig cfg = talbsw::fit_config(talbsw::choose_config(w, A.cols_cap, A.win),
+                                                   A.cols_cap, g_smem_optin[dev], A.win);
+    if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap, A.win) > g_smem_optin[dev])
         return TAL_EDOMAIN;  // a pair too long for the shared-memory rows
     e = talbsw::launch_config(A, cfg, g_num_sms[dev], g_smem_optin[dev], s);
     if (e != cudaSuccess) return TAL_ECUDA;

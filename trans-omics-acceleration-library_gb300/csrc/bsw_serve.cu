@@ -13,10 +13,11 @@
 //   tick (worker)             when a slot is free, every admitted request not
 //                             yet running becomes one tick on the slot's own
 //                             stream: wait for their copies, upload the tick's
-//                             request table, sort all their pairs into length
-//                             bins on the device, one persistent launch per
-//                             non-empty bin, copy the results back, record
-//                             the slot's event;
+//                             request table, sort all their pairs into
+//                             segments (length bin x band class) on the
+//                             device, one persistent launch per non-empty
+//                             segment side by side on forked streams, copy
+//                             the results back, record the slot's event;
 //   completion (worker)       a finished slot's requests get their status
 //                             (per request: the kernels record errors per
 //                             request in the table), their pool regions are
@@ -57,10 +58,10 @@ int64_t steady_ns() {
         .count();
 }
 
-int host_bin(int len2) {
+int host_seg(int len2, int w) {
     int b = 0;
     while (b < kNumBins - 1 && len2 > bin_upper(b)) b++;
-    return b;
+    return seg_index(b, seg_cls(b, w));
 }
 
 // First-fit allocator of byte ranges in [0, cap), 256-byte granules, with
@@ -121,7 +122,7 @@ struct Request {
     const int32_t *wpair = nullptr;
     int n = 0, w = 0, bits = 0;
     long long rlo = 0, rhi = 0, qlo = 0, qhi = 0;  // byte windows of the caller's buffers
-    int bins[kNumBins] = {};
+    int segs[kNumSegs] = {};  // pairs per segment
     // one region, in the device pool and (pageable callers) in the staging:
     // pairs | ref window | qer window | bands
     size_t off_pairs = 0, off_ref = 0, off_qer = 0, off_w = 0, bytes = 0;
@@ -278,8 +279,7 @@ int tal_bsw_server::launch_tick(Slot &sl) {
     const int max_pairs = cfg.max_tick_pairs;
     int nreq = 0;
     long long total = 0;
-    int bins[kNumBins] = {};
-    int wmax = 0;
+    int segs[kNumSegs] = {};
     while (nreq < (int)ready.size() && nreq < kMaxTickRequests) {
         Request *r = ready[nreq];
         if (nreq > 0 && total + r->n > max_pairs) break;
@@ -298,8 +298,7 @@ int tal_bsw_server::launch_tick(Slot &sl) {
         d.bits = r->bits;
         d.err = 0;
         d.pad_ = 0;
-        for (int b = 0; b < kNumBins; b++) bins[b] += r->bins[b];
-        wmax = std::max(wmax, r->w);
+        for (int g = 0; g < kNumSegs; g++) segs[g] += r->segs[g];
         total += r->n;
         nreq++;
     }
@@ -318,12 +317,18 @@ int tal_bsw_server::launch_tick(Slot &sl) {
     sb.order_req = reinterpret_cast<int32_t *>(sl.order_req.p);
     sb.seg = reinterpret_cast<int32_t *>(sl.seg.p);
     sb.ctrl = reinterpret_cast<BatchCtrl *>(sl.ctrl.p);
-    if (e == cudaSuccess && total > 0) e = enqueue_sort(h, sb, nullptr, dreqs, nreq, (int)total, sl.stream);
+    LaunchArgs base;
+    memset(&base, 0, sizeof(base));
+    base.reqs = dreqs;
+    if (e == cudaSuccess && total > 0) e = enqueue_sort(h, sb, base, nreq, (int)total, sl.stream);
+    // a small tick cannot hide a lane walking a long pair behind other work:
+    // a handful of launches, pairs above 256 columns with G lanes each; a
+    // large tick runs like the batched form, one tuned launch per segment
     if (e == cudaSuccess && total > 0) {
-        LaunchArgs base;
-        memset(&base, 0, sizeof(base));
-        base.reqs = dreqs;
-        e = enqueue_bins_forked(h, sb, base, bins, (int)total, wmax, sl.fork, sl.stream);
+        if (total < cfg.latency_pairs)
+            e = enqueue_tick(h, sb, base, segs, 7, sl.fork, sl.stream);
+        else
+            e = enqueue_segs_forked(h, sb, base, segs, (int)total, 100, sl.fork, sl.stream, false);
     }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(sl.hreqs, dreqs, sizeof(ReqDesc) * nreq, cudaMemcpyDeviceToHost, sl.stream);
@@ -478,7 +483,8 @@ int tal_bsw_server_create(tal_bsw_handle src, const tal_bsw_server_config *cfg,
     if (!src || !out) return TAL_EINVAL;
     *out = nullptr;
     tal_bsw_server_config c = cfg ? *cfg : tal_bsw_server_config{};
-    if (c.slots == 0) c.slots = 2;
+    if (c.slots == 0) c.slots = 4;
+    if (c.latency_pairs == 0) c.latency_pairs = 131072;
     if (c.max_tick_pairs == 0) c.max_tick_pairs = 8 << 20;
     if (c.staging_bytes == 0) c.staging_bytes = (size_t)1 << 30;
     if (c.slots < 1 || c.slots > 4 || c.max_tick_pairs < 1) return TAL_EINVAL;
@@ -492,7 +498,7 @@ int tal_bsw_server_create(tal_bsw_handle src, const tal_bsw_server_config *cfg,
     {
         std::lock_guard<std::mutex> lk(src->mu);
         s->h->tuned = src->tuned;
-        for (int b = 0; b < kNumBins; b++) s->h->bin_cfg[b] = src->bin_cfg[b];
+        for (int g = 0; g < kNumSegs; g++) s->h->bin_cfg[g] = src->bin_cfg[g];
     }
     cudaError_t e = cudaSetDevice(s->h->device);
     size_t free_b = 0, total_b = 0;
@@ -522,7 +528,7 @@ int tal_bsw_server_create(tal_bsw_handle src, const tal_bsw_server_config *cfg,
         if (e == cudaSuccess) e = sl.counts.ensure(sizeof(int) * kNumBuckets);
         if (e == cudaSuccess) e = sl.order.ensure(sizeof(int32_t) * (size_t)c.max_tick_pairs);
         if (e == cudaSuccess) e = sl.order_req.ensure(sizeof(int32_t) * (size_t)c.max_tick_pairs);
-        if (e == cudaSuccess) e = sl.seg.ensure(sizeof(int32_t) * 2 * kNumBins);
+        if (e == cudaSuccess) e = sl.seg.ensure(sizeof(int32_t) * 2 * kNumSegs);
         if (e == cudaSuccess) e = sl.ctrl.ensure(sizeof(BatchCtrl));
         if (e == cudaSuccess) e = sl.dreqs.ensure(sizeof(ReqDesc) * kMaxTickRequests);
         if (e == cudaSuccess) e = sl.fork.create();
@@ -580,7 +586,7 @@ int tal_bsw_submit(tal_bsw_server_handle s, tal_seq_pair *pairs, const uint8_t *
         qlo = std::min<long long>(qlo, p.idq);
         rhi = std::max<long long>(rhi, (long long)p.idr + p.len1);
         qhi = std::max<long long>(qhi, (long long)p.idq + p.len2);
-        r->bins[host_bin(p.len2)]++;
+        r->segs[host_seg(p.len2, wpair ? wpair[k] : w)]++;
     }
     bool done_now = numPairs == 0 || bad >= 0;
     if (!done_now) {

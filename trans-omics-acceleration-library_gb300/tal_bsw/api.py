@@ -63,6 +63,9 @@ _SIGS = {
     "tal_bsw_autotune_reset": (ctypes.c_int, [ctypes.c_void_p]),
     "tal_bsw_bin_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "tal_bsw_segment_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_int)]),
     "tal_bsw_probe_int_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_double)]),
     "tal_bsw_now_ns": (ctypes.c_int64, []),
@@ -79,7 +82,8 @@ _SIGS = {
 class ServerConfig(ctypes.Structure):
     """tal_bsw_server_config; zero fields take the library's defaults."""
     _fields_ = [("pool_bytes", ctypes.c_size_t), ("staging_bytes", ctypes.c_size_t),
-                ("max_tick_pairs", ctypes.c_int32), ("slots", ctypes.c_int32)]
+                ("max_tick_pairs", ctypes.c_int32), ("slots", ctypes.c_int32),
+                ("latency_pairs", ctypes.c_int32), ("pad_", ctypes.c_int32)]
 
 
 class RequestInfo(ctypes.Structure):
@@ -209,6 +213,14 @@ class BandedPairWiseSW:
                                                  ctypes.byref(m)))
         return g.value, k.value, m.value
 
+    def segment_config(self, seg: int):
+        """(lanes per pair, columns per lane, largest query length, row ring)
+        of segment seg (length bin seg // 5, band class seg % 5)."""
+        g, k, m, w = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self._lib.tal_bsw_segment_config(self._h, int(seg), ctypes.byref(g), ctypes.byref(k),
+                                                     ctypes.byref(m), ctypes.byref(w)))
+        return g.value, k.value, m.value, w.value
+
     def sync(self) -> None:
         self._check(self._lib.tal_bsw_sync(self._h))
 
@@ -272,9 +284,10 @@ class BswServer:
     (the library reads and writes them until then)."""
 
     def __init__(self, bsw: BandedPairWiseSW, pool_bytes: int = 0, staging_bytes: int = 0,
-                 max_tick_pairs: int = 0, slots: int = 0):
+                 max_tick_pairs: int = 0, slots: int = 0, latency_pairs: int = 0):
         self._lib = core_lib()
-        cfg = ServerConfig(int(pool_bytes), int(staging_bytes), int(max_tick_pairs), int(slots))
+        cfg = ServerConfig(int(pool_bytes), int(staging_bytes), int(max_tick_pairs), int(slots),
+                           int(latency_pairs), 0)
         s = ctypes.c_void_p()
         rc = self._lib.tal_bsw_server_create(bsw._h, ctypes.byref(cfg), ctypes.byref(s))
         if rc != TAL_OK:
