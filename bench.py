@@ -171,6 +171,17 @@ class ClockSampler:
                                     if r[3].replace(".", "").isdigit()), default=None)}
 
 
+def segment_configs(bsw):
+    """[lanes per pair, columns per lane, max query, ring] of every segment."""
+    import tal_bsw
+    out = []
+    while True:
+        try:
+            out.append(list(bsw.segment_config(len(out))))
+        except tal_bsw.TalBswError:
+            return out
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -365,7 +376,7 @@ def run_ours(args):
     batched = {"value": round(total_cells / t_batched / 1e9, 3), "unit": UNIT,
                "pairs_per_s": round(total_pairs / t_batched, 1),
                "ms_per_step": round(t_batched * 1e3, 3),
-               "segments": [list(bsw.segment_config(k)) for k in range(105)],
+               "segments": segment_configs(bsw),
                "note": "device-resident batched call (sort into segments = length bin x band "
                        "class, one persistent launch per segment on forked streams, one CUDA "
                        "graph); segments: [lanes per pair, columns per lane, max query, row ring]; "

@@ -126,13 +126,13 @@ int tal_bsw_autotune_reset(tal_bsw_handle h);
 int tal_bsw_bin_config(tal_bsw_handle h, int bin, int *lanes_per_pair, int *cols_per_lane,
                        int *max_len2);
 
-/* The configuration of segment `seg` (0..104) of the batched form.  A
- * segment is a length bin x band class (class c < 4: pairs with
- * 2w + 12 <= 64 << c, which the lane kernel scores in a ring of 64 << c
- * columns; class 4: whole rows); segments 0..10 are the whole-row bins of
- * queries above 384 columns, longest first, then all other segments, bins
- * longest first.  max_len2: the bin's largest query; window: the ring in
- * columns (0: whole rows, or not the lane kernel). */
+/* The configuration of segment `seg` (0..146) of the batched form.  A
+ * segment is a length bin x band class (class c < 6: pairs with
+ * 2w + 12 <= 64 << c, scored in rings of 64 << c columns; class 6: whole
+ * rows); segments 0..10 are the whole-row bins of queries above 384 columns,
+ * longest first, then all other segments, bins longest first.  max_len2: the
+ * bin's largest query; window: the ring in columns (0: whole rows).  Returns
+ * TAL_EINVAL past the last segment. */
 int tal_bsw_segment_config(tal_bsw_handle h, int seg, int *lanes_per_pair, int *cols_per_lane,
                            int *max_len2, int *window);
 

@@ -25,7 +25,7 @@ std::mutex atomic_mu;
 // did not finish together (a divergent exit).
 static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps) {
     size_t wbytes = G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap, A.win)
-                           : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G);
+                           : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G, A.win);
     std::vector<unsigned char> smem(wbytes * warps + 64, 0xA5);  // poisoned, like fresh smem
     // warps run one after another; the 32 lanes of a warp are fibers
     int divergent = 0;

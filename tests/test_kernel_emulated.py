@@ -124,3 +124,42 @@ def test_emulated_row_ring_wraps_on_long_queries():
         e, g = outputs(exp), outputs(got)
         bad = np.nonzero((e != g).any(1))[0]
         assert bad.size == 0, f"w={w} win={win}: pair {bad[0]}: emu {g[bad[0]].tolist()} oracle {e[bad[0]].tolist()}"
+
+
+@pytest.mark.parametrize("f", FILES, ids=os.path.basename)
+def test_emulated_group_kernel_with_row_ring(f):
+    """G lanes per pair with power-of-two rings as small as the band allows
+    (strips read and write column chunks through the ring; the head
+    re-derivation's reads below the band come from the frozen-column record)."""
+    d = np.load(f)
+    P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+    n = min(d["inputs"].shape[0], 6 if "c4" in f else 16)
+    p = d["inputs"][:n]
+    w = d["w"]
+    bits = int(d["bits"])
+    G, K = [(4, 4), (8, 4), (16, 4), (32, 4), (8, 2)][sum(os.path.basename(f).encode()) % 5]
+    wmax = int(np.max(w[:n])) if np.ndim(w) else int(w)
+    win = simt_emu.window_for(max(wmax, 0))
+    kw = dict(bits=bits, K=K, G=G, warps=2, win=win)
+    if np.ndim(w):
+        got, ef, _ = simt_emu.run(p, d["ref"], d["qer"], 0, P, wpair=w[:n], **kw)
+    else:
+        got, ef, _ = simt_emu.run(p, d["ref"], d["qer"], int(w), P, **kw)
+    assert ef == 0
+    e, g = outputs(d["expected"][:n]), outputs(got)
+    bad = np.nonzero((e != g).any(1))[0]
+    assert bad.size == 0, f"G={G} win={win}: pair {bad[0]}: emu {g[bad[0]].tolist()} ref {e[bad[0]].tolist()}"
+
+
+@pytest.mark.parametrize("G", [4, 8, 32])
+def test_emulated_group_ring_wraps_on_long_queries(G):
+    from tal_bsw import synth
+    b = synth.generate(synth.C2, 32)
+    P = synth.C2.params()
+    for w, win in ((100, 256), (20, 64)):
+        exp = oracle.vector(b.pairs, b.ref, b.qer, w, P, bits=16, lanes=1)
+        got, ef, _ = simt_emu.run(b.pairs, b.ref, b.qer, w, P, bits=16, K=4, G=G, warps=2, win=win)
+        assert ef == 0
+        e, g = outputs(exp), outputs(got)
+        bad = np.nonzero((e != g).any(1))[0]
+        assert bad.size == 0, f"G={G} w={w} win={win}: pair {bad[0]}: emu {g[bad[0]].tolist()} oracle {e[bad[0]].tolist()}"

@@ -170,17 +170,24 @@ cudaError_t enqueue_tick(tal_bsw_ctx *h, const SortBufs &sb, const LaunchArgs &b
                          const int *count, int lane_bin, BinFork &f, cudaStream_t s) {
     cudaError_t e = cudaEventRecord(f.fork, s);
     int k = 0;
-    // one G launch over the consecutive segments [s0, s1] of bin b
+    // one G launch over the consecutive segments [s0, s1] of bin b, with the
+    // largest ring its non-empty segments need (whole rows if any needs them)
     auto g_launch = [&](int s0, int s1, int b) {
-        int n = 0;
-        for (int sg = s0; sg <= s1; sg++) n += count[sg];
+        int n = 0, win = 0;
+        bool rows = false;
+        for (int sg = s0; sg <= s1; sg++) {
+            if (count[sg] <= 0) continue;
+            n += count[sg];
+            if (seg_window(sg) == 0) rows = true;
+            win = std::max(win, seg_window(sg));
+        }
         if (n <= 0 || e != cudaSuccess) return;
         e = cudaStreamWaitEvent(f.st[k], f.fork, 0);
         LaunchArgs A = seg_launch_args(h, sb, base, s0, n);
         A.nseg = s1 - s0 + 1;
         A.cols_cap = bin_cols(h, b);
-        A.win = 0;
-        const KConfig cfg = fit_config(latency_config(A.cols_cap, 0), A.cols_cap, h->smem_optin, 0);
+        A.win = rows ? 0 : win;
+        const KConfig cfg = fit_config(latency_config(A.cols_cap, A.win), A.cols_cap, h->smem_optin, A.win);
         if (e == cudaSuccess) e = launch_config(A, cfg, h->num_sms, h->smem_optin, f.st[k]);
         h->launches++;
         if (e == cudaSuccess) e = cudaEventRecord(f.join[k], f.st[k]);
@@ -596,14 +603,14 @@ int tal_bsw_segment_config(tal_bsw_handle h, int seg, int *lanes_per_pair, int *
     if (lanes_per_pair) *lanes_per_pair = c.G;
     if (cols_per_lane) *cols_per_lane = c.K;
     if (max_len2) *max_len2 = bin_cols(h, seg_bin(seg));
-    if (window) *window = c.G == 1 ? seg_window(seg) : 0;
+    if (window) *window = seg_window(seg);
     return TAL_OK;
 }
 
 int tal_bsw_bin_config(tal_bsw_handle h, int bin, int *lanes_per_pair, int *cols_per_lane,
                        int *max_len2) {
     if (bin < 0 || bin >= kNumBins) return TAL_EINVAL;
-    return tal_bsw_segment_config(h, seg_index(bin, kNumCls - 1), lanes_per_pair, cols_per_lane,
+    return tal_bsw_segment_config(h, seg_index(bin, kRingCls), lanes_per_pair, cols_per_lane,
                                   max_len2, nullptr);
 }
 

@@ -52,18 +52,20 @@ __host__ __device__ constexpr int bin_upper(int b) {
         default: return 32767;
     }
 }
-// Band classes within a length bin: class c < 4 holds pairs whose band fits
-// a ring of 64 << c columns (2w + 12 <= 64 << c) in the lane kernel; class 4
-// holds whole rows.  A class whose ring would be no smaller than the bin's
-// whole rows folds into class 4.  A segment is a (length bin, band class).
-constexpr int kNumCls = 5;
+// Band classes within a length bin: class c < kRingCls holds pairs whose
+// band fits a ring of 64 << c columns (2w + 12 <= 64 << c; rings of 64 ..
+// 2,048 columns), class kRingCls holds whole rows.  A class whose ring would
+// be no smaller than the bin's whole rows folds into the whole-row class.
+// A segment is a (length bin, band class).
+constexpr int kRingCls = 6;
+constexpr int kNumCls = kRingCls + 1;
 __host__ __device__ inline int seg_cls(int b, long long w) {
-    for (int c = 0; c < kNumCls - 1; c++) {
+    for (int c = 0; c < kRingCls; c++) {
         const long long W = 64LL << c;
-        if (W >= bin_upper(b) + 4) return kNumCls - 1;
+        if (W >= bin_upper(b) + 4) return kRingCls;
         if (2 * w + 12 <= W) return c;
     }
-    return kNumCls - 1;
+    return kRingCls;
 }
 
 // Segment order of the sort (positions 0..kNumSegs-1): first the whole-row
@@ -72,31 +74,31 @@ __host__ __device__ inline int seg_cls(int b, long long w) {
 // in order.  Each bin's segments are consecutive there, and so is any run of
 // bins from bin 0 up, so a launch can take one bin, or all bins up to a
 // length, as one range.
-constexpr int kRowSegs = 11;                  // positions 0..10: bins 20..10, class 4
-constexpr int kNumSegs = kRowSegs + 44 + 50;  // bins 20..10: classes 0-3; bins 9..0: classes 0-4
+constexpr int kRowSegs = 11;  // positions 0..10: bins 20..10, whole rows
+constexpr int kNumSegs = kRowSegs + 11 * kRingCls + 10 * kNumCls;
 __host__ __device__ inline int seg_index(int b, int c) {
-    if (c == kNumCls - 1 && b >= 10) return 20 - b;
-    return kRowSegs + (b >= 10 ? (20 - b) * 4 : 44 + (9 - b) * 5) + c;
+    if (c == kRingCls && b >= 10) return 20 - b;
+    return kRowSegs + (b >= 10 ? (20 - b) * kRingCls : 11 * kRingCls + (9 - b) * kNumCls) + c;
 }
 __host__ __device__ inline int seg_bin(int s) {
     if (s < kRowSegs) return 20 - s;
     const int r = s - kRowSegs;
-    return r < 44 ? 20 - r / 4 : 9 - (r - 44) / 5;
+    return r < 11 * kRingCls ? 20 - r / kRingCls : 9 - (r - 11 * kRingCls) / kNumCls;
 }
 __host__ __device__ inline int seg_class(int s) {
-    if (s < kRowSegs) return kNumCls - 1;
+    if (s < kRowSegs) return kRingCls;
     const int r = s - kRowSegs;
-    return r < 44 ? r % 4 : (r - 44) % 5;
+    return r < 11 * kRingCls ? r % kRingCls : (r - 11 * kRingCls) % kNumCls;
 }
 // First and last position of bin b's ring / lane segments (not its
 // whole-row segment when b >= 10).
 __host__ __device__ inline int seg_first(int b) { return seg_index(b, 0); }
-__host__ __device__ inline int seg_last(int b) { return seg_index(b, b >= 10 ? kNumCls - 2 : kNumCls - 1); }
-// The lane kernel's ring for segment s: 64 << c for class c < 4, 0 (whole
-// rows) for class 4.
+__host__ __device__ inline int seg_last(int b) { return seg_index(b, b >= 10 ? kRingCls - 1 : kRingCls); }
+// The ring of segment s: 64 << c columns for class c < kRingCls, 0 (whole
+// rows) otherwise.  The lane kernel's query ring is win / 8 words.
 __host__ __device__ inline int seg_window(int s) {
     const int c = seg_class(s);
-    return c < kNumCls - 1 ? (64 << c) : 0;
+    return c < kRingCls ? (64 << c) : 0;
 }
 
 constexpr int kRowBuckets = 512;  // len1 / 8, capped

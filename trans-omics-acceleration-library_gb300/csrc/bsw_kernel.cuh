@@ -225,58 +225,26 @@ struct VecIO<4> {
 constexpr int KPAD = 4;  // widest strip's columns per lane: row padding
 
 // Shared-memory footprint of one pair's rows, in bytes (16-byte aligned parts):
-// H_h and F (int32 each) and the query as 16-bit byte-permute selectors.  The
-// target is read from global memory, one base per row.
-__host__ __device__ __forceinline__ size_t smem_hh_bytes(int cols_cap) {
+// H_h and F (int32 each) and the query as 16-bit byte-permute selectors, for
+// whole rows of cols_cap columns or -- win > 0 -- rings of win columns (a
+// power of two; column j in slot j & (win - 1)).  The target is read from
+// global memory, one base per row.
+__host__ __device__ __forceinline__ size_t smem_hh_bytes(int cols_cap, int win = 0) {
+    if (win > 0) return (size_t)win * 4;
     return ((size_t)(cols_cap + 2 + KPAD) * 4 + 15) & ~(size_t)15;
 }
-__host__ __device__ __forceinline__ size_t smem_q_bytes(int cols_cap) {
+__host__ __device__ __forceinline__ size_t smem_q_bytes(int cols_cap, int win = 0) {
+    if (win > 0) return (size_t)win * 2;
     return ((size_t)(cols_cap + KPAD + 8) * 2 + 15) & ~(size_t)15;
 }
-__host__ __device__ __forceinline__ size_t pair_smem_bytes(int cols_cap, int rows_cap) {
+__host__ __device__ __forceinline__ size_t pair_smem_bytes(int cols_cap, int rows_cap, int win = 0) {
     (void)rows_cap;
-    return 2 * smem_hh_bytes(cols_cap) + smem_q_bytes(cols_cap);
+    return 2 * smem_hh_bytes(cols_cap, win) + smem_q_bytes(cols_cap, win);
 }
 // one warp = 32/G pairs
-__host__ __device__ __forceinline__ size_t warp_smem_bytes(int cols_cap, int rows_cap, int G) {
-    return (size_t)(32 / G) * pair_smem_bytes(cols_cap, rows_cap);
-}
-
-// Stage len bytes at window offset `off` of the device window src (window
-// length buf_bytes, 16-byte aligned start) into shared dst, G lanes sharing
-// the work (lane gl), with 16-byte vector loads; each base code b is stored as
-// b * MUL + ADD (the query as a ready-made byte-permute selector).
-// Returns true in a lane that saw a byte above 4.
-template <int G, typename T, uint32_t MUL, uint32_t ADD>
-__device__ __forceinline__ bool stage_bases(T *dst, const uint8_t *src, int len,
-                                            size_t buf_bytes, size_t off, int gl) {
-    bool bad = false;
-    if (len <= 0) return false;
-    // aligned 16-byte chunks covering [off, off+len), never past the window
-    size_t a0 = off & ~(size_t)15;
-    size_t a1 = (off + (size_t)len + 15) & ~(size_t)15;
-    if (a1 > (buf_bytes & ~(size_t)15)) a1 = buf_bytes & ~(size_t)15;
-    for (size_t c = a0 + (size_t)gl * 16; c < a1; c += (size_t)G * 16) {
-        uint4 v = *reinterpret_cast<const uint4 *>(src + c);
-        uint32_t wv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int b = 0; b < 16; b++) {
-            size_t pos = c + b;
-            if (pos >= off && pos < off + (size_t)len) {
-                uint32_t byte = (wv[b >> 2] >> ((b & 3) * 8)) & 0xffu;
-                if (byte > 4u) bad = true;
-                dst[pos - off] = (T)(byte * MUL + ADD);
-            }
-        }
-    }
-    // tail bytes past the last whole 16-byte unit of the buffer
-    size_t done = a1 > off ? a1 - off : 0;
-    for (size_t p = done + gl; p < (size_t)len; p += G) {
-        uint32_t byte = src[off + p];
-        if (byte > 4u) bad = true;
-        dst[p] = (T)(byte * MUL + ADD);
-    }
-    return bad;
+__host__ __device__ __forceinline__ size_t warp_smem_bytes(int cols_cap, int rows_cap, int G,
+                                                           int win = 0) {
+    return (size_t)(32 / G) * pair_smem_bytes(cols_cap, rows_cap, win);
 }
 
 constexpr int NEG = -(1 << 29);  // "minus infinity" for the E scan, no overflow
@@ -339,16 +307,17 @@ enum { STRIP_INTERIOR = 0, STRIP_EDGE = 1, STRIP_MASKED = 2 };
 template <int G, int K, int MODE>
 __device__ __forceinline__ void do_strip(const int base, const bool act, const int gl,
                                          RowState &r, const CellConsts &c, int *Hh, int *Fv,
-                                         const uint16_t *Qs) {
+                                         const uint16_t *Qs, const int wm) {
     const unsigned full = 0xffffffffu;
     const int j0 = base + gl * K;
+    const int s0 = j0 & wm;  // K-aligned, so the lane's K columns are contiguous slots
     int hv[K], fv[K];
     uint32_t qs[K];
     const bool ld = act && (MODE == STRIP_INTERIOR || j0 < r.end);
     if (ld) {
-        VecIO<K>::ld(Hh + j0, hv);
-        VecIO<K>::ld(Fv + j0, fv);
-        VecIO<K>::ldq(Qs + j0, qs);
+        VecIO<K>::ld(Hh + s0, hv);
+        VecIO<K>::ld(Fv + s0, fv);
+        VecIO<K>::ldq(Qs + s0, qs);
     } else {
 #pragma unroll
         for (int k = 0; k < K; k++) { hv[k] = 0; fv[k] = 0; qs[k] = 0x8880u; }
@@ -418,14 +387,14 @@ __device__ __forceinline__ void do_strip(const int base, const bool act, const i
     }
     if (ld) {
         if (MODE == STRIP_INTERIOR || (lo <= 0 && hi >= K)) {
-            VecIO<K>::st(Hh + j0, ho);
-            VecIO<K>::st(Fv + j0, fo);
+            VecIO<K>::st(Hh + s0, ho);
+            VecIO<K>::st(Fv + s0, fo);
         } else {
 #pragma unroll
             for (int k = 0; k < K; k++) {
                 if (k >= lo && k < hi) {
-                    Hh[j0 + k] = ho[k];
-                    Fv[j0 + k] = fo[k];
+                    Hh[s0 + k] = ho[k];
+                    Fv[s0 + k] = fo[k];
                 }
             }
         }
@@ -451,13 +420,13 @@ __device__ __forceinline__ unsigned group_max(unsigned v) {
 // Warp-uniform loop; each pair searches with its own G lanes.
 template <int G>
 __device__ __forceinline__ int scan_first_nz(const int *Hh, const int *Fv, int lo, int hi,
-                                             bool act, int gl, int gshift, unsigned gbits) {
+                                             bool act, int gl, int gshift, unsigned gbits, int wm) {
     int found = hi;
     bool srch = act && lo < hi;
     int b = lo;
     while (__any_sync(0xffffffffu, srch)) {
         const int j = b + gl;
-        const bool nz = srch && j < hi && ((Hh[j] | Fv[j]) != 0);
+        const bool nz = srch && j < hi && ((Hh[j & wm] | Fv[j & wm]) != 0);
         const unsigned m = (__ballot_sync(0xffffffffu, nz) & gbits) >> gshift;
         if (srch) {
             if (m) { found = b + __ffs(m) - 1; srch = false; }
@@ -469,13 +438,13 @@ __device__ __forceinline__ int scan_first_nz(const int *Hh, const int *Fv, int l
 // Last column of [lo, hi] with H_h | F non-zero, scanning down; lo-1 if none.
 template <int G>
 __device__ __forceinline__ int scan_last_nz(const int *Hh, const int *Fv, int lo, int hi,
-                                            bool act, int gl, int gshift, unsigned gbits) {
+                                            bool act, int gl, int gshift, unsigned gbits, int wm) {
     int found = lo - 1;
     bool srch = act && hi >= lo;
     int t = hi;
     while (__any_sync(0xffffffffu, srch)) {
         const int j = t - gl;
-        const bool nz = srch && j >= lo && ((Hh[j] | Fv[j]) != 0);
+        const bool nz = srch && j >= lo && ((Hh[j & wm] | Fv[j & wm]) != 0);
         const unsigned m = (__ballot_sync(0xffffffffu, nz) & gbits) >> gshift;
         if (srch) {
             if (m) { found = t - (__ffs(m) - 1); srch = false; }
@@ -488,7 +457,10 @@ __device__ __forceinline__ int scan_last_nz(const int *Hh, const int *Fv, int lo
 // Per-pair state, uniform across the pair's G lanes.
 struct PairState {
     DevPair *pp;
+    const uint8_t *Qg;   // the query in global memory (staged lazily)
     int pidx, req, nrow, ncol, i;
+    int initc, v1;       // next column to initialise; its row-0 value base
+    int fend, p;         // frozen columns [nbeg, fend) seen; p: first nonzero of them, or -1
     int beg, end, nbeg, nend, head, tail;
     int maxScore, x, y, gscore, max_ie, max_off;
     int h0e, o_delE, e_delE, bandE, wk, qlenE, mlen, zdropE;
@@ -507,11 +479,13 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
     const int wib = threadIdx.x >> 5;
     const int g = lane / G, gl = lane % G, gshift = g * G;
     const unsigned gbits = (G == 32) ? full : (((1u << G) - 1u) << gshift);
-    const size_t pbytes = pair_smem_bytes(A.cols_cap, A.rows_cap);
+    const size_t pbytes = pair_smem_bytes(A.cols_cap, A.rows_cap, A.win);
     unsigned char *pbase = smem_raw + ((size_t)wib * NG + g) * pbytes;
     int *Hh = reinterpret_cast<int *>(pbase);
-    int *Fv = reinterpret_cast<int *>(pbase + smem_hh_bytes(A.cols_cap));
-    uint16_t *Qs = reinterpret_cast<uint16_t *>(pbase + 2 * smem_hh_bytes(A.cols_cap));
+    int *Fv = reinterpret_cast<int *>(pbase + smem_hh_bytes(A.cols_cap, A.win));
+    uint16_t *Qs = reinterpret_cast<uint16_t *>(pbase + 2 * smem_hh_bytes(A.cols_cap, A.win));
+    const bool ring = A.win > 0;
+    const int wm = ring ? A.win - 1 : -1;  // column -> slot mask (-1: whole rows)
     const uint8_t *Tg = nullptr;  // this pair's target in global memory
     int tnext = 0;                // its next row's base, loaded one row ahead
     const KernelParams P = A.P;
@@ -578,21 +552,13 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
                      (long long)idr + len1 <= src.ref_hi && (long long)idq + len2 <= src.qer_hi;
                 if (!ok) {
                     if (gl == 0) report_error(A, req, ERR_DOMAIN, pidx);
-                } else if (len2 > A.cols_cap) {
+                } else if (ring ? (2LL * wcall + 12 > A.win && len2 + 4 > A.win)
+                                : (len2 > A.cols_cap)) {
                     ok = false;
                     if (gl == 0) report_error(A, req, ERR_CAPACITY, pidx);
                 }
             }
-            bool st = take && ok;
-            // stage the bases (query as PRMT selectors)
-            bool bad = stage_bases<G, uint16_t, 0x1111u, 0x8880u>(
-                Qs, src.qer, st ? len2 : 0, (size_t)(src.qer_hi - src.qer_lo),
-                st ? (size_t)(idq - src.qer_lo) : 0, gl);
-            const unsigned bm = __ballot_sync(full, bad) & gbits;
-            if (st && bm) {
-                if (gl == 0) report_error(A, req, ERR_BASE, pidx);
-                st = false;
-            }
+            const bool st = take && ok;
             if (st) {
                 // per-pair constants (smithWatermanBatchWrapper16/8 set-up)
                 const int sh = is8 ? 24 : 16, msk = is8 ? 0xff : 0xffff;
@@ -601,6 +567,7 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
                 ps.nrow = len1; ps.ncol = len2; ps.i = 0; ps.ncells = 0;
                 Tg = src.ref + (idr - src.ref_lo);
                 tnext = len1 > 0 ? Tg[0] : 0;
+                ps.Qg = src.qer + (idq - src.qer_lo);
                 ps.h0e = wrapS(wrapU(h0in, msk), sh);
                 ps.o_delE = P.o_del;
                 ps.e_delE = P.e_del;
@@ -634,18 +601,11 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
                 ps.maxScore = ps.h0e; ps.x = 0; ps.y = 0; ps.gscore = -1; ps.max_off = 0;
                 ps.max_ie = 0;
                 ps.beg = 0; ps.end = len2; ps.nbeg = 0; ps.nend = len2;
-                // row 0 values H_h[k] and F[k] = 0 (:2839-2879)
-                const int v1 = (ps.h0e > oe_ins) ? wrapS(ps.h0e - oe_ins, sh) : 0;
-                const int top = len2 > 1 ? len2 : 1;
-                for (int k = gl; k <= top; k += G) {
-                    int hv;
-                    if (k == 0) hv = ps.h0e;
-                    else if (k == 1) hv = v1;
-                    else if (k < len2) hv = imax(v1 - (k - 1) * P.e_ins, 0);
-                    else hv = 0;
-                    Hh[k] = hv;
-                    Fv[k] = 0;
-                }
+                // row 0 values H_h[k] and F[k] = 0 (:2839-2879), set lazily
+                // as columns come within reach
+                ps.v1 = (ps.h0e > oe_ins) ? wrapS(ps.h0e - oe_ins, sh) : 0;
+                ps.initc = 0;
+                ps.fend = 0; ps.p = -1;
                 active = true;
             }
             __syncwarp();
@@ -658,6 +618,35 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
         const int sh = ps.sh, msk = ps.msk;
         const int i = ps.i;
         const int i1 = wrapS(i + 1, sh);
+        // columns up to i + wk + 3 can be touched by this row (band end + 2):
+        // their row-0 values and query selectors, by the pair's G lanes
+        {
+            bool badq = false;
+            if (rowact) {
+                const int lim = imin(imax(ps.ncol, 1), i + ps.wk + 3);
+                for (int k = ps.initc + gl; k <= lim; k += G) {
+                    int hv;
+                    if (k == 0) hv = ps.h0e;
+                    else if (k == 1) hv = ps.v1;
+                    else if (k < ps.ncol) hv = imax(ps.v1 - (k - 1) * P.e_ins, 0);
+                    else hv = 0;
+                    Hh[k & wm] = hv;
+                    Fv[k & wm] = 0;
+                    if (k < ps.ncol) {
+                        const uint32_t qc = ps.Qg[k];
+                        badq |= qc > 4u;
+                        Qs[k & wm] = (uint16_t)(qc * 0x1111u + 0x8880u);
+                    }
+                }
+                ps.initc = imax(ps.initc, lim + 1);
+            }
+            if ((__ballot_sync(full, badq) & gbits) && rowact) {  // a query base code above 4
+                if (gl == 0) report_error(A, ps.req, ERR_BASE, ps.pidx);
+                active = false;
+                rowact = false;
+            }
+            __syncwarp();
+        }
         int beg = 0, end = 0, h10init = 0;
         bool changed = false;
         if (rowact) {
@@ -679,10 +668,19 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             ps.tail = wrapS(t, sh);
             changed = ps.head != phead || ps.tail != ptail;
         }
+        // columns that left the band since the last row are frozen: note the
+        // first nonzero one at or after nbeg (16-bit head re-derivation)
+        {
+            const int lo = imax(ps.fend, ps.nbeg);
+            const bool fr = rowact && !ps.is8 && ps.p < 0 && lo < beg;
+            const int f = scan_first_nz<G>(Hh, Fv, lo, beg, fr, gl, gshift, gbits, wm);
+            if (fr && f < beg) ps.p = f;
+            if (rowact) ps.fend = imax(ps.fend, beg);
+        }
         // trimming (:3091-3112): zero [beg, min(end, head))
         if (rowact && changed) {
             const int hi = imin(end, ps.head);
-            for (int l = beg + gl; l < hi; l += G) { Hh[l] = 0; Fv[l] = 0; }
+            for (int l = beg + gl; l < hi; l += G) { Hh[l & wm] = 0; Fv[l & wm] = 0; }
         }
         __syncwarp();
         // row exit status (:3119-3129); outputs freeze once a pair exits
@@ -735,9 +733,9 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             const int want = (!act || inner) ? STRIP_INTERIOR : (needmask ? STRIP_MASKED : STRIP_EDGE);
             if (act && s == nstr - 1) lastint = inner;
             const int mode = (int)__reduce_max_sync(full, (unsigned)want);
-            if (mode == STRIP_INTERIOR) do_strip<G, K, STRIP_INTERIOR>(base, act, gl, r, cc, Hh, Fv, Qs);
-            else if (mode == STRIP_EDGE) do_strip<G, K, STRIP_EDGE>(base, act, gl, r, cc, Hh, Fv, Qs);
-            else do_strip<G, K, STRIP_MASKED>(base, act, gl, r, cc, Hh, Fv, Qs);
+            if (mode == STRIP_INTERIOR) do_strip<G, K, STRIP_INTERIOR>(base, act, gl, r, cc, Hh, Fv, Qs, wm);
+            else if (mode == STRIP_EDGE) do_strip<G, K, STRIP_EDGE>(base, act, gl, r, cc, Hh, Fv, Qs, wm);
+            else do_strip<G, K, STRIP_MASKED>(base, act, gl, r, cc, Hh, Fv, Qs, wm);
         }
         __syncwarp();
         const uint32_t key = group_max<G>(r.key);
@@ -749,8 +747,8 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             const int h10 = ran ? hlast : h10init;
             const bool m = (ps.head > jl) || (jl > ps.tail);
             if (gl == 0 && jl <= ps.ncol + 1) {
-                Hh[jl] = m ? 0 : h10;
-                Fv[jl] = 0;
+                Hh[jl & wm] = m ? 0 : h10;
+                Fv[jl & wm] = 0;
             }
             // gscore at the query's last column (:3177-3195); it is in the
             // band exactly when end == ncol, and then it is column end-1
@@ -790,10 +788,14 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
         }
         // band narrowing (:3235-3260)
         {
-            const int f = scan_first_nz<G>(Hh, Fv, beg, end, rowact, gl, gshift, gbits);
-            const int L = scan_last_nz<G>(Hh, Fv, beg, end, rowact, gl, gshift, gbits);
+            const int f = scan_first_nz<G>(Hh, Fv, beg, end, rowact, gl, gshift, gbits, wm);
+            const int L = scan_last_nz<G>(Hh, Fv, beg, end, rowact, gl, gshift, gbits, wm);
             if (rowact) {
-                if (f > beg) ps.nbeg = f - 1;
+                if (f > beg) {  // nbeg >= beg: no frozen columns at or after it yet
+                    ps.nbeg = f - 1;
+                    ps.fend = ps.nbeg;
+                    ps.p = -1;
+                }
                 ps.nend = (L + 2 < ps.ncol) ? L + 2 : ps.ncol;
             }
         }
@@ -802,8 +804,19 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
         {
             const int B = ps.is8 ? beg : ps.nbeg;
             const int E = ps.is8 ? end : ps.nend;
-            const int f2 = scan_first_nz<G>(Hh, Fv, B, E, rowact && E > B, gl, gshift, gbits);
-            const int L2 = scan_last_nz<G>(Hh, Fv, B, E, rowact && E >= B, gl, gshift, gbits);
+            // the frozen columns [B, beg) answer from p; the rest is live
+            const bool use_p = B < beg && ps.p >= 0 && ps.p < E;
+            const int Bl = B < beg ? imin(beg, E) : B;
+            int f2 = scan_first_nz<G>(Hh, Fv, Bl, E, rowact && E > B && !use_p, gl, gshift, gbits, wm);
+            if (use_p) f2 = ps.p;
+            // a cell with H > 0 left a nonzero in [beg + 1, end]: this scan
+            // stops inside the band
+            const int L2 = scan_last_nz<G>(Hh, Fv, imax(B, beg), E, rowact && E >= B, gl, gshift, gbits, wm);
+            if (rowact && ring && E >= B && L2 < beg) {  // would have read a reused ring slot
+                if (gl == 0) report_error(A, ps.req, ERR_CAPACITY, ps.pidx);
+                active = false;
+                rowact = false;
+            }
             if (rowact) {
                 if (E > B && f2 > B) ps.head = wrapS(f2, sh);
                 int index = ps.tail;

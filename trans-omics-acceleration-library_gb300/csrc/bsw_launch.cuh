@@ -86,7 +86,7 @@ inline cudaError_t resident_blocks(const void *kern, int threads, size_t smem, s
 template <int G, int K>
 inline cudaError_t launch_gk(const LaunchArgs &A, int num_sms, size_t smem_optin, cudaStream_t s) {
     auto kern = bsw_kernel<G, K>;
-    const size_t wbytes = warp_smem_bytes(A.cols_cap, A.rows_cap, G);
+    const size_t wbytes = warp_smem_bytes(A.cols_cap, A.rows_cap, G, A.win);
     int wpb = 4;
     while (wpb > 1 && (size_t)wpb * wbytes * 2 > smem_optin) wpb >>= 1;
     const size_t smem = (size_t)wpb * wbytes;
@@ -144,7 +144,7 @@ inline KConfig latency_config(int cols_cap, int win) {
 // Shared memory one warp of the chosen configuration needs.
 inline size_t config_smem(const KConfig &c, int cols_cap, int rows_cap, int win = 0) {
     if (c.G == 1) return lane_warp_smem_bytes(cols_cap, win);
-    return warp_smem_bytes(cols_cap, rows_cap, c.G);
+    return warp_smem_bytes(cols_cap, rows_cap, c.G, win);
 }
 
 // Widens the lanes per pair (fewer pairs per warp, less shared memory per
