@@ -23,12 +23,16 @@ _PARAM_KEYS = ("o_del", "e_del", "o_ins", "e_ins", "zdrop", "end_bonus", "a", "b
 _libs: Dict[str, ctypes.CDLL] = {}
 
 
+ORACLE_SRCS = ("bsw_oracle.cpp", "sw_oracle.cpp")
+
+
 def build(force: bool = False) -> str:
-    """Compile the restatement (g++, host only)."""
-    src = os.path.join(HERE, "bsw_oracle.cpp")
-    if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
+    """Compile the restatements (g++, host only)."""
+    srcs = [os.path.join(HERE, f) for f in ORACLE_SRCS]
+    if force or not os.path.exists(ORACLE_SO) or \
+            os.path.getmtime(ORACLE_SO) < max(os.path.getmtime(f) for f in srcs):
         os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
-        subprocess.check_call(["g++", "-O3", "-fPIC", "-shared", "-pthread", "-o", ORACLE_SO, src])
+        subprocess.check_call(["g++", "-O3", "-fPIC", "-shared", "-pthread", "-o", ORACLE_SO, *srcs])
     return ORACLE_SO
 
 
@@ -47,6 +51,9 @@ def _oracle():
         lib.oracle_bsw_vector.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_int32, ctypes.c_int]
+        lib.oracle_sw.restype = ctypes.c_int
+        lib.oracle_sw.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                  ctypes.c_int64, ctypes.c_int]
         lib.oracle_bsw_scalar.restype = ctypes.c_int
         lib.oracle_bsw_scalar.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
@@ -169,3 +176,52 @@ def routed(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w, params: Dict[
             if sel.size:
                 out[sel] = vector(out[sel], ref, qer, int(wv), params, bits=b, nthreads=nthreads)
     return out
+
+
+# ---------------------------------------------------------------- unbanded SW
+SW_KEYS = ("match", "mismatch", "open", "extend")
+
+
+def sw(pairs: np.ndarray, seqbuf: np.ndarray, stride: int, params: Dict[str, int],
+       nthreads: int = 1) -> np.ndarray:
+    """The reference's unbanded Smith-Waterman scores restated
+    (oracle/sw_oracle.cpp); returns a scored copy of the 12-byte pairs."""
+    out = np.ascontiguousarray(pairs).copy()
+    pv = np.array([int(params[k]) for k in SW_KEYS], np.int32)
+    rc = _oracle().oracle_sw(_ptr(pv), _ptr(out), out.shape[0], _ptr(seqbuf), int(stride),
+                             int(nthreads))
+    if rc != 0:
+        raise ValueError("oracle_sw rejected its arguments")
+    return out
+
+
+def sw_ref_available() -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "libsw_ref_avx512.so"))
+
+
+def _sw_ref_lib():
+    if "sw_ref" not in _libs:
+        lib = ctypes.CDLL(os.path.join(REF_DIR, "libsw_ref_avx512.so"))
+        lib.ref_sw_run.restype = ctypes.c_int
+        lib.ref_sw_run.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_void_p,
+                                                        ctypes.c_int32]
+        lib.ref_sw_max_len.restype = ctypes.c_int
+        _libs["sw_ref"] = lib
+    return _libs["sw_ref"]
+
+
+def sw_reference(pairs: np.ndarray, seqbuf: np.ndarray, params: Dict[str, int],
+                 bits: int = 16) -> np.ndarray:
+    """The reference's own PairWiseSW_8/_16/_32::getScores (bits 8, 16, 32) or
+    its scalar smithWatermanOnePairWrapper (bits 0) on a copy of pairs."""
+    out = np.ascontiguousarray(pairs).copy()
+    rc = _sw_ref_lib().ref_sw_run(int(bits), *[int(params[k]) for k in SW_KEYS], _ptr(out),
+                                  _ptr(seqbuf), out.shape[0])
+    if rc != 0:
+        raise RuntimeError("ref_sw_run failed")
+    return out
+
+
+def sw_ref_max_len(bits: int) -> int:
+    """The reference's MAX_SEQ_LEN for a precision (its sequence stride)."""
+    return int(_sw_ref_lib().ref_sw_max_len(int(bits)))

@@ -28,5 +28,20 @@ if grep -q avx512bw /proc/cpuinfo; then
   build -mavx512bw avx512 &
 fi
 build -mavx2 avx2 &
+
+# The unbanded Smith-Waterman classes (src/alignment/Smith-Waterman).  Their
+# header defines its own __rdtsc, which clashes with the compiler's: each
+# reference source is compiled through a one-line wrapper that includes
+# <immintrin.h> first and renames the header's copy.
+REF_SW="${TAL_REFERENCE_ROOT:-/root/reference}/src/alignment/Smith-Waterman"
+if [ -f "$REF_SW/PairWiseSW_16.cpp" ] && grep -q avx512bw /proc/cpuinfo; then
+  mkdir -p "$OUT/sw_wrap"
+  for f in PairWiseSW PairWiseSW_8 PairWiseSW_16 PairWiseSW_32; do
+    printf '#include <immintrin.h>\n#define __rdtsc tal_ref_rdtsc\n#include "%s/%s.cpp"\n' \
+      "$REF_SW" "$f" > "$OUT/sw_wrap/$f.cpp"
+  done
+  g++ -O2 -fPIC -shared -mavx512bw -fopenmp -w -I"$REF_SW" "$OUT"/sw_wrap/*.cpp \
+      "$HERE/ref_sw_shim.cpp" -o "$OUT/libsw_ref_avx512.so" &
+fi
 wait
 ls "$OUT"/*.so
