@@ -60,6 +60,9 @@ def parse_args():
     ap.add_argument("--mixed-pairs", type=int, default=None,
                     help="pairs of the mixed-length workload (default: all 10,000,000)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
+    ap.add_argument("--no-full-sw", action="store_true", help="skip the unbanded Smith-Waterman section")
+    ap.add_argument("--sw-pairs", type=int, default=100_000,
+                    help="pairs of the unbanded Smith-Waterman workload")
     ap.add_argument("--serve-loads", type=float, nargs="+", default=[0.1, 0.3, 0.5, 0.7, 0.9])
     ap.add_argument("--serve-requests", type=int, default=300, help="requests per load point")
     ap.add_argument("--serve-plain-loads", type=float, nargs="+", default=[0.1, 0.7])
@@ -421,6 +424,9 @@ def run_ours(args):
     if not args.no_mixed:
         log("mixed-length plain vs batched")
         result["mixed"] = run_mixed(args, bsw, dist)
+    if not args.no_full_sw:
+        log("unbanded Smith-Waterman")
+        result["full_sw"] = run_full_sw(args, dist)
     if not args.no_serving:
         log("serving loop")
         peak = result.get("mixed", {}).get("batched", {}).get("pairs_per_s")
@@ -653,6 +659,69 @@ def run_serving(args, dist, peak_pairs_per_s):
             "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3)})
     out["plain_outputs_match"] = bool((tal_bsw.outputs(hp[touched]) == tal_bsw.outputs(exp[touched])).all())
     bsw.close()
+    return out
+
+
+def run_full_sw(args, dist):
+    """The unbanded Smith-Waterman scorer (PairWiseSW_16::getScores drop-in):
+    GCUPS = sum of len1 * len2 (the reference driver's SW_cells) per second,
+    device-resident and end to end through getScores on pinned host buffers."""
+    import torch
+    from tal_bsw import swdata
+    from tal_bsw.sw import PairWiseSW_16
+    n = args.sw_pairs
+    b = swdata.generate(n, 200, 1000, bits=16, seed=31 + dist.rank)
+    P = dict(match=1, mismatch=-4, open=-6, extend=-1)
+    cells = b.cells
+    out = {"workload": f"{n} pairs, len1 U[200,1000], len2 = len1 + U[-10,10], 4% substitutions, "
+                       "match 1, mismatch -4, open -6, extend -1, PairWiseSW_16 semantics"}
+    with PairWiseSW_16(P["match"], P["mismatch"], P["open"], P["extend"], device=dist.local) as sw:
+        stream = torch.cuda.ExternalStream(sw.stream)
+        dp = torch.from_numpy(b.pairs.view(np.uint8).reshape(-1).copy()).cuda()
+        ds = torch.from_numpy(b.seqbuf).cuda()
+        torch.cuda.synchronize()
+        for _ in range(2):
+            sw.scores_device(dp.data_ptr(), ds.data_ptr(), ds.numel(), n)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        steps = 3
+        dist.barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            sw.scores_device(dp.data_ptr(), ds.data_ptr(), ds.numel(), n)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = dist.max(e0.elapsed_time(e1) / 1e3 / steps)
+        out["device"] = {"value": round(dist.sum(cells) / t / 1e9, 2), "unit": "GCUPS",
+                         "ms_per_step": round(t * 1e3, 3)}
+        hp = torch.empty(b.pairs.nbytes, dtype=torch.uint8, pin_memory=True)
+        hs = torch.empty(b.seqbuf.nbytes, dtype=torch.uint8, pin_memory=True)
+        hp.numpy()[:] = b.pairs.view(np.uint8).reshape(-1)
+        hs.numpy()[:] = b.seqbuf
+        hpairs = hp.numpy().view(swdata.SW_DTYPE)
+        sw.getScores(hpairs, hs.numpy(), n, 1)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            sw.getScores(hpairs, hs.numpy(), n, 1)
+        te = dist.max((time.perf_counter() - t0) / steps)
+        out["e2e"] = {"value": round(dist.sum(cells) / te / 1e9, 2), "unit": "GCUPS",
+                      "ms_per_step": round(te * 1e3, 3),
+                      "h2d_bytes_per_step": int(b.pairs.nbytes + b.seqbuf.nbytes),
+                      "d2h_bytes_per_step": int(b.pairs.nbytes)}
+        dev_scores = dp.cpu().numpy().view(swdata.SW_DTYPE)["score"]
+        out["outputs_match_device_path"] = bool((dev_scores == hpairs["score"]).all())
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        import oracle
+        k = min(n, 2000)
+        nth = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        exp = oracle.sw(b.pairs[:k], b.seqbuf, b.stride, P, nthreads=nth)
+        dt = time.perf_counter() - t0
+        sample_cells = int((b.pairs["len1"][:k].astype(np.int64) * b.pairs["len2"][:k]).sum())
+        out["cpu_baseline"] = {"value": round(sample_cells / dt / 1e9, 4), "unit": "GCUPS", "cores": nth,
+                               "kind": "port", "sample": f"first {k} pairs, oracle restatement"}
+        out["outputs_match_oracle_sample"] = bool((exp["score"] == hpairs["score"][:k]).all())
     return out
 
 

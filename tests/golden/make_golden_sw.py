@@ -1,4 +1,4 @@
-"""Regenerates the unbanded Smith-Waterman golden fixtures (sw*.npz) from the
+"""Regenerates the unbanded Smith-Waterman golden fixtures (sw/*.npz) from the
 reference itself: PairWiseSW_8 / _16 / _32::getScores, AVX-512BW build made by
 oracle/build_ref.sh from the reference sources.  Each fixture holds seeded
 12-byte SeqPair records, the sequence buffer (stride = the precision's
@@ -23,7 +23,8 @@ PARAMS = {"bwa": dict(match=1, mismatch=-4, open=-6, extend=-1),
 
 def save(name, b, P, bits):
     exp = oracle.sw_reference(b.pairs, b.seqbuf, P, bits=bits)
-    np.savez_compressed(os.path.join(HERE, name + ".npz"), inputs=b.pairs, seqbuf=b.seqbuf,
+    os.makedirs(os.path.join(HERE, "sw"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "sw", name + ".npz"), inputs=b.pairs, seqbuf=b.seqbuf,
                         stride=np.int32(b.stride), bits=np.int32(bits),
                         param_keys=np.array(KEYS), param_vals=np.array([P[k] for k in KEYS], np.int32),
                         expected=exp)

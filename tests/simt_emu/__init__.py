@@ -15,7 +15,8 @@ _lib = None
 
 def build(force=False):
     srcs = [os.path.join(HERE, "emu.cpp"), os.path.join(HERE, "fake", "cuda_runtime.h"),
-            os.path.join(CSRC, "bsw_kernel.cuh"), os.path.join(CSRC, "bsw_lane.cuh")]
+            os.path.join(CSRC, "bsw_kernel.cuh"), os.path.join(CSRC, "bsw_lane.cuh"),
+            os.path.join(CSRC, "sw_kernel.cuh")]
     if force or not os.path.exists(SO) or os.path.getmtime(SO) < max(os.path.getmtime(s) for s in srcs):
         os.makedirs(os.path.dirname(SO), exist_ok=True)
         subprocess.check_call(["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-pthread", "-w",
@@ -91,3 +92,22 @@ def window_for(w):
     while W < 2 * w + 12:
         W *= 2
     return W
+
+
+def run_sw(pairs, seqbuf, stride, params, bits=16, warps=2):
+    """The unbanded Smith-Waterman kernel, emulated; returns (pairs, flags, bad)."""
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+    out = np.ascontiguousarray(pairs).copy()
+    buf = np.ascontiguousarray(seqbuf)
+    pv = np.array([params[k] for k in ("match", "mismatch", "open", "extend")], np.int32)
+    lim = {8: 127, 16: 32767, 32: 2 ** 31 - 1}[bits]
+    bad = ctypes.c_longlong(0)
+    vp = ctypes.c_void_p
+    _lib.emu_sw_run.restype = ctypes.c_int
+    flags = _lib.emu_sw_run(vp(out.ctypes.data), int(out.shape[0]), vp(buf.ctypes.data),
+                            ctypes.c_longlong(buf.shape[0]), ctypes.c_longlong(stride),
+                            int(stride - 4), int(lim), vp(pv.ctypes.data), int(warps),
+                            ctypes.byref(bad))
+    return out, flags, bad.value

@@ -19,12 +19,17 @@ std::mutex atomic_mu;
 #define TALBSW_DYNAMIC_SMEM(name) unsigned char *name = simt::tl_smem
 #include "bsw_kernel.cuh"
 #include "bsw_lane.cuh"
+#include "sw_kernel.cuh"
 #include <functional>
 
 // Runs one launch of A (one block of `warps` warps); -1 if a warp's lanes
 // did not finish together (a divergent exit).
-static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps) {
-    size_t wbytes = G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap, A.win)
+// sw != nullptr: the unbanded Smith-Waterman kernel with those arguments
+// instead (G, K unused).
+static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
+                      const talsw::SwArgs *sw = nullptr) {
+    size_t wbytes = sw ? talsw::sw_warp_smem_bytes(sw->cols_cap)
+                  : G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap, A.win)
                            : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G, A.win);
     std::vector<unsigned char> smem(wbytes * warps + 64, 0xA5);  // poisoned, like fresh smem
     // warps run one after another; the 32 lanes of a warp are fibers
@@ -32,10 +37,10 @@ static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps) {
     for (int wi = 0; wi < warps; wi++) {
         simt::Warp *W = new simt::Warp();
         std::vector<std::vector<char>> stacks(32, std::vector<char>(1 << 18));
-        struct Arg { int t; simt::Warp *W; const talbsw::LaunchArgs *A; int G, K; unsigned char *sm; int warps; };
+        struct Arg { int t; simt::Warp *W; const talbsw::LaunchArgs *A; int G, K; unsigned char *sm; int warps; const talsw::SwArgs *sw; };
         static thread_local Arg args[32];
         for (int l = 0; l < 32; l++) {
-            args[l] = Arg{wi * 32 + l, W, &A, G, K, smem.data(), warps};
+            args[l] = Arg{wi * 32 + l, W, &A, G, K, smem.data(), warps, sw};
             getcontext(&W->lane_ctx[l]);
             W->lane_ctx[l].uc_stack.ss_sp = stacks[l].data();
             W->lane_ctx[l].uc_stack.ss_size = stacks[l].size();
@@ -48,6 +53,7 @@ static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps) {
                 simt::tl_gridDim.x = 1;
                 simt::tl_warp = a.W;
                 simt::tl_smem = a.sm;
+                if (a.sw) { talsw::sw_wave_kernel(*a.sw); a.W->done[a.t & 31] = true; return; }
                 if (a.G == 1) { const bool sym = a.A->P.o_del == a.A->P.o_ins && a.A->P.e_del == a.A->P.e_ins; int v = a.K == 4 ? 3 : a.K == 2 ? 2 : 1; if (!sym) v &= 1; if (v == 3) talbsw::bsw_lane_kernel<3>(*a.A); else if (v == 2) talbsw::bsw_lane_kernel<2>(*a.A); else if (v == 1) talbsw::bsw_lane_kernel<1>(*a.A); else talbsw::bsw_lane_kernel<0>(*a.A); a.W->done[a.t & 31] = true; return; }
                 switch (a.G * 10 + a.K) {
                     case 44: talbsw::bsw_kernel<4, 4>(*a.A); break;
@@ -145,4 +151,32 @@ extern "C" int emu_bsw_run_reqs(int nreq, talbsw::DevPair **pairs, const uint8_t
         req_bad[r] = R[r].bad;
     }
     return rc;
+}
+
+
+// The unbanded Smith-Waterman kernel over n 12-byte pairs; seqbuf holds the
+// whole caller buffer (window [0, seq_bytes)).  params: match, mismatch,
+// open, extend.  Returns the kernel's error flags (bad index in *bad).
+extern "C" int emu_sw_run(void *pairs, int n, const uint8_t *seqbuf, long long seq_bytes,
+                          long long stride, int maxlen, int score_lim, const int32_t *params,
+                          int warps, long long *bad) {
+    talsw::SwArgs S;
+    std::memset(&S, 0, sizeof(S));
+    S.pairs = static_cast<talsw::SwPair *>(pairs);
+    S.seq = seqbuf; S.seq_lo = 0; S.seq_hi = seq_bytes; S.stride = stride;
+    S.n = n;
+    int cols = 1;
+    for (int k = 0; k < n; k++) cols = std::max<int>(cols, S.pairs[k].len2);
+    S.cols_cap = cols;
+    S.maxlen = maxlen;
+    S.score_lim = score_lim;
+    S.match = params[0]; S.mismatch = params[1]; S.open = params[2]; S.ext = params[3];
+    int counter = 0, flags = 0;
+    long long badi = (long long)INT64_MAX;
+    S.work_counter = &counter; S.err_flags = &flags; S.err_index = &badi;
+    talbsw::LaunchArgs A;
+    std::memset(&A, 0, sizeof(A));
+    const int rc = run_launch(A, 1, 4, warps, &S);
+    *bad = badi;
+    return rc < 0 ? -1 : flags;
 }

@@ -152,3 +152,4 @@ inline int __viaddmin_s32(int a, int b, int c) { int s = a + b; return s < c ? s
 inline int __viaddmax_s32(int a, int b, int c) { int s = a + b; return s > c ? s : c; }
 inline int __viaddmax_s32_relu(int a, int b, int c) { int s = a + b; int m = s > c ? s : c; return m > 0 ? m : 0; }
 inline int __vimax3_s32(int a, int b, int c) { int m = a > b ? a : b; return m > c ? m : c; }
+inline int __vimax3_s32_relu(int a, int b, int c) { int m = __vimax3_s32(a, b, c); return m > 0 ? m : 0; }

@@ -67,9 +67,19 @@ def test_ctypes_structs_match_the_header(tmp_path):
     field offsets as gcc lays out include/tal_bsw.h)."""
     import subprocess
     from tal_bsw.api import RequestInfo, ServerConfig, ServerStats, _Params
+    from tal_bsw.sw import _SwParams
+    import numpy as np
+    from tal_bsw.swdata import SW_DTYPE
+
+    class _SwPair(ctypes.Structure):
+        _fields_ = [(n, {"<i4": ctypes.c_int32, "<i2": ctypes.c_int16}[SW_DTYPE.fields[n][0].str])
+                    for n in SW_DTYPE.names]
+        _pack_ = 1
     structs = {"tal_bsw_server_config": ServerConfig, "tal_bsw_request_info": RequestInfo,
-               "tal_bsw_server_stats": ServerStats, "tal_bsw_params": _Params}
-    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "tal_bsw.h"', "int main(void) {"]
+               "tal_bsw_server_stats": ServerStats, "tal_bsw_params": _Params,
+               "tal_sw_params": _SwParams, "tal_sw_pair": _SwPair}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "tal_bsw.h"', '#include "tal_sw.h"',
+             "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
         for f, _ in py._fields_:

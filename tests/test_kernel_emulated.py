@@ -163,3 +163,17 @@ def test_emulated_group_ring_wraps_on_long_queries(G):
         e, g = outputs(exp), outputs(got)
         bad = np.nonzero((e != g).any(1))[0]
         assert bad.size == 0, f"G={G} w={w} win={win}: pair {bad[0]}: emu {g[bad[0]].tolist()} oracle {e[bad[0]].tolist()}"
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLDEN, "sw", "*.npz"))), ids=os.path.basename)
+def test_emulated_sw_kernel_matches_golden(f):
+    """The unbanded Smith-Waterman wavefront kernel (one warp per pair, rows
+    in bands of 32, shuffles between rows) against the reference's scores."""
+    d = np.load(f)
+    P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+    n = min(d["inputs"].shape[0], 12)
+    got, flags, _ = simt_emu.run_sw(d["inputs"][:n], d["seqbuf"], int(d["stride"]), P,
+                                    bits=int(d["bits"]), warps=2)
+    assert flags == 0
+    assert (got["score"] == d["expected"]["score"][:n]).all(), \
+        (got["score"].tolist(), d["expected"]["score"][:n].tolist())

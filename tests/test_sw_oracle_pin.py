@@ -57,7 +57,7 @@ def test_scalar_reference_equals_vector():
             oracle.sw_reference(b.pairs, b.seqbuf, P, bits=32)["score"]).all()
 
 
-@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLDEN, "sw*.npz"))),
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLDEN, "sw", "*.npz"))),
                          ids=os.path.basename)
 def test_oracle_equals_golden(f):
     d = np.load(f)
