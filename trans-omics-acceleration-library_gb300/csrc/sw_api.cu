@@ -85,11 +85,12 @@ int run_locked(tal_sw_ctx *h, tal_sw_pair *d_pairs, const uint8_t *d_seq, long l
     const size_t smem = wbytes * wpb;
     if (smem > h->smem_optin) return sfail(h, TAL_EDOMAIN, "sequences too long for shared memory");
     int bps = 0;
-    e = talbsw::resident_blocks((const void *)talsw::sw_wave_kernel, 32 * wpb, smem, h->smem_optin, &bps);
+    auto kern = talsw::sw_wave_kernel<talsw::kSwRows>;
+    e = talbsw::resident_blocks((const void *)kern, 32 * wpb, smem, h->smem_optin, &bps);
     if (e != cudaSuccess || bps < 1) return sfail(h, TAL_ECUDA, "occupancy query");
     long long blocks = (long long)bps * h->num_sms;
     blocks = std::min<long long>(blocks, ((long long)n + wpb - 1) / wpb);
-    talsw::sw_wave_kernel<<<(unsigned)std::max<long long>(blocks, 1), 32 * wpb, smem, h->stream>>>(A);
+    kern<<<(unsigned)std::max<long long>(blocks, 1), 32 * wpb, smem, h->stream>>>(A);
     if ((e = cudaGetLastError()) != cudaSuccess) return sfail(h, TAL_ECUDA, cudaGetErrorString(e));
     SwCtrl out;
     e = cudaMemcpyAsync(&out, c, sizeof(out), cudaMemcpyDeviceToHost, h->stream);

@@ -10,13 +10,15 @@
 // E = open at the start of a row; the row above the first holds H = 0, F = open.
 // The answer is the largest H.
 //
-// Lane t of the warp owns row 32b + t of band b and walks the columns one
-// step behind lane t - 1 (an anti-diagonal wavefront): at step s it computes
-// column s - t, taking H and F' of the row above from lane t - 1 through a
-// shuffle (lane t - 1 computed that column at step s - 1) and its diagonal H
-// from the previous step; E stays in the lane.  Lane 31 writes its row's H
-// and F' to shared memory, where lane 0 of the next band reads them.  Every
-// cell is computed once, in int32 (exact inside the range the host checks).
+// Lane t of the warp owns rows [R*t, R*t + R) of a band of 32*R rows and walks
+// the columns one step behind lane t - 1 (an anti-diagonal wavefront): at
+// step s it computes column s - t of its R rows, top to bottom, taking H and
+// F' of the row above its block from lane t - 1 through a shuffle (lane t - 1
+// computed that column at step s - 1); each row keeps its diagonal H and its
+// E in registers.  Lane 31 writes its bottom row's H and F' to shared memory,
+// where lane 0 of the next band reads them.  R rows per lane share one
+// shuffle pair, one query load and the loop control.  Every cell is computed
+// once, in int32 (exact inside the range the host checks).
 #pragma once
 
 #include <stdint.h>
@@ -58,6 +60,9 @@ __host__ __device__ __forceinline__ size_t sw_warp_smem_bytes(int cols_cap) {
     return ((size_t)cols_cap * 9 + 16 + 15) & ~(size_t)15;
 }
 
+constexpr int kSwRows = 8;  // rows per lane
+
+template <int R>
 __global__ void __launch_bounds__(128) sw_wave_kernel(SwArgs A) {
     TALBSW_DYNAMIC_SMEM(smem_raw);
     const unsigned full = 0xffffffffu;
@@ -104,31 +109,46 @@ __global__ void __launch_bounds__(128) sw_wave_kernel(SwArgs A) {
         }
         __syncwarp();
         int best = 0;
-        for (int rb = 0; rb < nrow; rb += 32) {
-            const int r = rb + lane;
-            const bool rv = r < nrow;
-            const int c1 = rv ? (int)s1[r] : -1;  // never equal to a byte
-            int e = open, hdiag = 0, hout = 0, fout = open;
+        for (int rb = 0; rb < nrow; rb += 32 * R) {
+            int c1[R], e[R], hdiag[R];
+            bool rv[R];
+#pragma unroll
+            for (int k = 0; k < R; k++) {
+                const int r = rb + lane * R + k;
+                rv[k] = r < nrow;
+                c1[k] = rv[k] ? (int)s1[r] : -1;  // never equal to a byte
+                e[k] = open;
+                hdiag[k] = 0;
+            }
+            int hout = 0, fout = open;
             const int steps = ncol + 31;
             for (int s = 0; s < steps; s++) {
-                int hup = __shfl_up_sync(full, hout, 1);
-                int fin = __shfl_up_sync(full, fout, 1);
+                int hu = __shfl_up_sync(full, hout, 1);
+                int fu = __shfl_up_sync(full, fout, 1);
                 const int j = s - lane;
                 if (lane == 0 && j < ncol) {
-                    hup = Hrow[j];
-                    fin = Frow[j];
+                    hu = Hrow[j];
+                    fu = Frow[j];
                 }
-                if (rv && j >= 0 && j < ncol) {
-                    const int m = hdiag + ((c1 == (int)Q[j]) ? match : mismatch);
-                    const int h = __vimax3_s32_relu(m, e, fin);
-                    best = best > h ? best : h;
-                    const int t = h + open;
-                    e = __viaddmax_s32(e, ext, t);
-                    fout = __viaddmax_s32(fin, ext, t);
-                    hout = h;
-                    hdiag = hup;
+                if (rv[0] && j >= 0 && j < ncol) {
+                    const int q = Q[j];
+#pragma unroll
+                    for (int k = 0; k < R; k++) {
+                        if (rv[k]) {  // hu, fu: H and F' of the row above, this column
+                            const int m = hdiag[k] + ((c1[k] == q) ? match : mismatch);
+                            const int h = __vimax3_s32_relu(m, e[k], fu);
+                            best = best > h ? best : h;
+                            const int t = h + open;
+                            e[k] = __viaddmax_s32(e[k], ext, t);
+                            fu = __viaddmax_s32(fu, ext, t);
+                            hdiag[k] = hu;
+                            hu = h;
+                        }
+                    }
+                    hout = hu;
+                    fout = fu;
                     if (lane == 31) {
-                        Hrow[j] = h;
+                        Hrow[j] = hout;
                         Frow[j] = fout;
                     }
                 }
