@@ -94,14 +94,19 @@ def window_for(w):
     return W
 
 
-def run_sw(pairs, seqbuf, stride, params, bits=16, warps=2):
-    """The unbanded Smith-Waterman kernel, emulated; returns (pairs, flags, bad)."""
+def run_sw(pairs, seqbuf, stride, params, bits=16, warps=2, packed=None, order=None):
+    """The unbanded Smith-Waterman kernel, emulated (packed: two pairs per warp
+    in 16x2 lanes; default as the library picks, for 8/16-bit; order: the
+    work order, pair indices); returns (pairs, flags, bad)."""
+    if packed is None:
+        packed = bits != 32 and params["match"] - params["mismatch"] <= 32768
     global _lib
     if _lib is None:
         _lib = ctypes.CDLL(build())
     out = np.ascontiguousarray(pairs).copy()
     buf = np.ascontiguousarray(seqbuf)
     pv = np.array([params[k] for k in ("match", "mismatch", "open", "extend")], np.int32)
+    ordv = None if order is None else np.ascontiguousarray(order, np.int32)
     lim = {8: 127, 16: 32767, 32: 2 ** 31 - 1}[bits]
     bad = ctypes.c_longlong(0)
     vp = ctypes.c_void_p
@@ -109,5 +114,7 @@ def run_sw(pairs, seqbuf, stride, params, bits=16, warps=2):
     flags = _lib.emu_sw_run(vp(out.ctypes.data), int(out.shape[0]), vp(buf.ctypes.data),
                             ctypes.c_longlong(buf.shape[0]), ctypes.c_longlong(stride),
                             int(stride - 4), int(lim), vp(pv.ctypes.data), int(warps),
+                            int(bool(packed)),
+                            vp(ordv.ctypes.data) if ordv is not None else None,
                             ctypes.byref(bad))
     return out, flags, bad.value

@@ -26,9 +26,11 @@ std::mutex atomic_mu;
 // did not finish together (a divergent exit).
 // sw != nullptr: the unbanded Smith-Waterman kernel with those arguments
 // instead (G, K unused).
+static int sw_packed = 0;  // the unbanded kernel: 1 = two pairs per warp (16x2)
+
 static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
                       const talsw::SwArgs *sw = nullptr) {
-    size_t wbytes = sw ? talsw::sw_warp_smem_bytes(sw->cols_cap)
+    size_t wbytes = sw ? (sw_packed ? talsw::sw2_warp_smem_bytes(sw->cols_cap) : talsw::sw_warp_smem_bytes(sw->cols_cap))
                   : G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap, A.win)
                            : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G, A.win);
     std::vector<unsigned char> smem(wbytes * warps + 64, 0xA5);  // poisoned, like fresh smem
@@ -53,7 +55,7 @@ static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
                 simt::tl_gridDim.x = 1;
                 simt::tl_warp = a.W;
                 simt::tl_smem = a.sm;
-                if (a.sw) { talsw::sw_wave_kernel<talsw::kSwRows>(*a.sw); a.W->done[a.t & 31] = true; return; }
+                if (a.sw) { if (sw_packed) talsw::sw_wave2_kernel<talsw::kSwRows>(*a.sw); else talsw::sw_wave_kernel<talsw::kSwRows>(*a.sw); a.W->done[a.t & 31] = true; return; }
                 if (a.G == 1) { const bool sym = a.A->P.o_del == a.A->P.o_ins && a.A->P.e_del == a.A->P.e_ins; int v = a.K == 4 ? 3 : a.K == 2 ? 2 : 1; if (!sym) v &= 1; if (v == 3) talbsw::bsw_lane_kernel<3>(*a.A); else if (v == 2) talbsw::bsw_lane_kernel<2>(*a.A); else if (v == 1) talbsw::bsw_lane_kernel<1>(*a.A); else talbsw::bsw_lane_kernel<0>(*a.A); a.W->done[a.t & 31] = true; return; }
                 switch (a.G * 10 + a.K) {
                     case 44: talbsw::bsw_kernel<4, 4>(*a.A); break;
@@ -159,12 +161,14 @@ extern "C" int emu_bsw_run_reqs(int nreq, talbsw::DevPair **pairs, const uint8_t
 // open, extend.  Returns the kernel's error flags (bad index in *bad).
 extern "C" int emu_sw_run(void *pairs, int n, const uint8_t *seqbuf, long long seq_bytes,
                           long long stride, int maxlen, int score_lim, const int32_t *params,
-                          int warps, long long *bad) {
+                          int warps, int packed, const int32_t *order, long long *bad) {
+    sw_packed = packed;
     talsw::SwArgs S;
     std::memset(&S, 0, sizeof(S));
     S.pairs = static_cast<talsw::SwPair *>(pairs);
     S.seq = seqbuf; S.seq_lo = 0; S.seq_hi = seq_bytes; S.stride = stride;
     S.n = n;
+    S.order = order;
     int cols = 1;
     for (int k = 0; k < n; k++) cols = std::max<int>(cols, S.pairs[k].len2);
     S.cols_cap = cols;

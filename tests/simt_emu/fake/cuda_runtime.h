@@ -5,6 +5,7 @@
 #pragma once
 #include <atomic>
 #include <climits>
+#include <cstdlib>
 #include <ucontext.h>
 #include <cstdint>
 #include <cstring>
@@ -122,6 +123,9 @@ inline unsigned __reduce_min_sync(unsigned, unsigned v) {
     return r;
 }
 inline void __syncwarp(unsigned = 0xffffffffu) { simt::tl_warp->barrier(simt::lane()); }
+// Block barriers appear only in kernels the emulator never runs (the work
+// order sort); warps here run one after another, so none could be honoured.
+inline void __syncthreads() { std::abort(); }
 inline int __ffs(unsigned x) { return x ? __builtin_ctz(x) + 1 : 0; }
 inline int __clz(unsigned x) { return x ? __builtin_clz(x) : 32; }
 inline int __popc(unsigned x) { return __builtin_popcount(x); }
@@ -153,3 +157,23 @@ inline int __viaddmax_s32(int a, int b, int c) { int s = a + b; return s > c ? s
 inline int __viaddmax_s32_relu(int a, int b, int c) { int s = a + b; int m = s > c ? s : c; return m > 0 ? m : 0; }
 inline int __vimax3_s32(int a, int b, int c) { int m = a > b ? a : b; return m > c ? m : c; }
 inline int __vimax3_s32_relu(int a, int b, int c) { int m = __vimax3_s32(a, b, c); return m > 0 ? m : 0; }
+// 16x2 forms: each 16-bit half on its own
+inline int sw_lo16(unsigned v) { return (int)(short)(v & 0xffffu); }
+inline int sw_hi16(unsigned v) { return (int)(short)(v >> 16); }
+inline unsigned sw_pack16(int lo, int hi) { return ((unsigned)lo & 0xffffu) | ((unsigned)hi << 16); }
+inline unsigned __viaddmax_s16x2(unsigned a, unsigned b, unsigned c) {
+    auto f = [](int x, int y, int z) { int s = (int)(short)(x + y); return s > z ? s : z; };
+    return sw_pack16(f(sw_lo16(a), sw_lo16(b), sw_lo16(c)), f(sw_hi16(a), sw_hi16(b), sw_hi16(c)));
+}
+inline unsigned __viaddmax_s16x2_relu(unsigned a, unsigned b, unsigned c) {
+    auto f = [](int x, int y, int z) { int s = (int)(short)(x + y); s = s > z ? s : z; return s > 0 ? s : 0; };
+    return sw_pack16(f(sw_lo16(a), sw_lo16(b), sw_lo16(c)), f(sw_hi16(a), sw_hi16(b), sw_hi16(c)));
+}
+inline unsigned __vimax3_s16x2_relu(unsigned a, unsigned b, unsigned c) {
+    auto f = [](int x, int y, int z) { int m = x > y ? x : y; m = m > z ? m : z; return m > 0 ? m : 0; };
+    return sw_pack16(f(sw_lo16(a), sw_lo16(b), sw_lo16(c)), f(sw_hi16(a), sw_hi16(b), sw_hi16(c)));
+}
+inline unsigned __vimin3_u16x2(unsigned a, unsigned b, unsigned c) {
+    auto f = [](unsigned x, unsigned y, unsigned z) { unsigned m = x < y ? x : y; return m < z ? m : z; };
+    return (f(a & 0xffffu, b & 0xffffu, c & 0xffffu)) | (f(a >> 16, b >> 16, c >> 16) << 16);
+}

@@ -73,3 +73,23 @@ def test_gpu_device_resident_and_refusals():
     with pytest.raises(TalBswError) as ei:
         PairWiseSW_16(1, -4, 6, -1, device=0)   # a positive gap weight
     assert ei.value.status == TAL_EINVAL
+
+
+@pytest.mark.parametrize("bits,P", [
+    (16, dict(match=300, mismatch=-32468, open=-32000, extend=-768)),   # match - mismatch = 2^15
+    (16, dict(match=300, mismatch=-32768, open=-32000, extend=-768)),   # past it: 32-bit lanes
+    (8, dict(match=1, mismatch=-128, open=-100, extend=-28)),
+])
+def test_gpu_weights_at_the_element_limits(bits, P):
+    """Weights at the limits of the element type, lengths up to what the score
+    bound allows, ragged neighbours: scores equal the oracle's."""
+    rng = np.random.default_rng(bits)
+    hi = {8: 100, 16: 100}[bits]
+    b = swdata.generate(2001, 0, hi, bits=bits, seed=5)
+    b.pairs["len1"] = rng.integers(0, hi + 1, b.n)
+    b.pairs["len2"] = rng.integers(0, hi + 1, b.n)
+    exp = oracle.sw(b.pairs, b.seqbuf, b.stride, P, nthreads=8)
+    got = b.pairs.copy()
+    with _sw(P, bits) as sw:
+        sw.getScores(got, b.seqbuf, b.n, 1)
+    assert (got["score"] == exp["score"]).all()

@@ -172,8 +172,63 @@ def test_emulated_sw_kernel_matches_golden(f):
     d = np.load(f)
     P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
     n = min(d["inputs"].shape[0], 12)
-    got, flags, _ = simt_emu.run_sw(d["inputs"][:n], d["seqbuf"], int(d["stride"]), P,
-                                    bits=int(d["bits"]), warps=2)
-    assert flags == 0
-    assert (got["score"] == d["expected"]["score"][:n]).all(), \
-        (got["score"].tolist(), d["expected"]["score"][:n].tolist())
+    bits = int(d["bits"])
+    for packed in ((False, True) if bits != 32 else (False,)):
+        got, flags, _ = simt_emu.run_sw(d["inputs"][:n], d["seqbuf"], int(d["stride"]), P,
+                                        bits=bits, warps=2, packed=packed)
+        assert flags == 0
+        assert (got["score"] == d["expected"]["score"][:n]).all(), \
+            (packed, got["score"].tolist(), d["expected"]["score"][:n].tolist())
+
+
+@pytest.mark.parametrize("bits,params", [
+    (16, dict(match=2, mismatch=-3, open=-5, extend=-1)),
+    (16, dict(match=300, mismatch=-32000, open=-30000, extend=-2768)),
+    (16, dict(match=300, mismatch=-32468, open=-32000, extend=-768)),
+    (8, dict(match=1, mismatch=-128, open=-100, extend=-28)),
+])
+def test_emulated_sw_two_pairs_per_warp_ragged(bits, params):
+    """Two pairs per warp in 16x2 lanes: neighbouring pairs of very different
+    lengths (empty ones too), an odd pair count, byte codes over the whole
+    0..255 range and weights at the element type's limits, against the
+    oracle; the 32-bit-lane kernel gives the same scores."""
+    from tal_bsw import swdata
+    rng = np.random.default_rng(7 + bits)
+    n = 13
+    hi = {8: 60, 16: 100}[bits]
+    b = swdata.generate(n, 0, hi, bits=bits, seed=bits)
+    b.seqbuf[:] = rng.integers(0, 256, b.seqbuf.size, dtype=np.uint8)
+    b.pairs["len1"] = rng.integers(0, hi + 1, n)
+    b.pairs["len2"] = rng.integers(0, hi + 1, n)
+    b.pairs["len1"][[0, 5]] = 0
+    b.pairs["len2"][[3, 8]] = 0
+    # seq2 a mutated copy of seq1 for pairs with high scores
+    for k in range(0, n, 2):
+        s = b.seqbuf.reshape(2 * n, -1)
+        s[2 * k + 1] = s[2 * k]
+        s[2 * k + 1, ::7] ^= 1
+    exp = oracle.sw(b.pairs, b.seqbuf, b.stride, params)
+    # the library's work order: longer sequence first, in buckets of 8
+    key = np.maximum(b.pairs["len1"], b.pairs["len2"]) >> 3
+    for packed in (True, False):
+        for order in (None, np.argsort(-key, kind="stable").astype(np.int32)):
+            got, flags, _ = simt_emu.run_sw(b.pairs, b.seqbuf, b.stride, params, bits=bits, warps=2,
+                                            packed=packed, order=order)
+            assert flags == 0
+            assert (got["score"] == exp["score"]).all(), (packed, got["score"].tolist(), exp["score"].tolist())
+
+
+def test_emulated_sw_two_pairs_per_warp_bad_pair():
+    """A pair outside the precision's range sits beside a good one in the
+    same warp: it raises the domain flag with its index, and its neighbour
+    is still scored."""
+    from tal_bsw import swdata
+    b = swdata.generate(6, 20, 40, bits=8, seed=3)
+    P = dict(match=1, mismatch=-1, open=-2, extend=-1)
+    b.pairs["len1"][3] = 100   # (min length + 1) * match above int8 is fine only below 127
+    b.pairs["len2"][3] = 130   # past the 8-bit kernel's longest sequence
+    exp = oracle.sw(b.pairs[[0, 1, 2, 4, 5]], b.seqbuf, b.stride, P)
+    got, flags, bad = simt_emu.run_sw(b.pairs, b.seqbuf, b.stride, P, bits=8, warps=2, packed=True,
+                                      order=np.array([5, 3, 0, 1, 2, 4], np.int32))
+    assert flags != 0 and bad == 3
+    assert (got["score"][[0, 1, 2, 4, 5]] == exp["score"]).all()

@@ -23,9 +23,12 @@ struct SwCtrl {
     int flags;
     long long bad;
     unsigned long long cells;
+    int hist[talsw::kSwBuckets];  // work-order buckets
 };
 
 int max_seq_len(int bits) { return bits == 8 ? 128 : 1024; }  // PairWiseSW_{8,16,32}.h
+
+constexpr int kSortMin = 256;  // batches from this size are scored in length order
 
 }  // namespace
 
@@ -34,7 +37,7 @@ struct tal_sw_ctx {
     int device = 0, num_sms = 0;
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
-    talbsw::DevBuf pairs, seq, ctrl;
+    talbsw::DevBuf pairs, seq, ctrl, order;
     std::mutex mu;
     std::string last_error;
     int64_t last_bad = -1;
@@ -60,7 +63,9 @@ int run_locked(tal_sw_ctx *h, tal_sw_pair *d_pairs, const uint8_t *d_seq, long l
     cudaError_t e;
     if ((e = h->ctrl.ensure(sizeof(SwCtrl))) != cudaSuccess)
         return sfail(h, TAL_ENOMEM, "control block");
-    SwCtrl init = {0, 0, LLONG_MAX, 0ull};
+    SwCtrl init;
+    memset(&init, 0, sizeof(init));
+    init.bad = LLONG_MAX;
     e = cudaMemcpyAsync(h->ctrl.p, &init, sizeof(init), cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return sfail(h, TAL_ECUDA, cudaGetErrorString(e));
     SwCtrl *c = reinterpret_cast<SwCtrl *>(h->ctrl.p);
@@ -76,20 +81,37 @@ int run_locked(tal_sw_ctx *h, tal_sw_pair *d_pairs, const uint8_t *d_seq, long l
     A.maxlen = max_seq_len(bits) - 4;
     A.score_lim = lim;
     A.match = p.w_match; A.mismatch = p.w_mismatch; A.open = p.w_open; A.ext = p.w_extend;
+    // work order by length, longest first (small batches keep theirs)
+    if (n >= kSortMin) {
+        if ((e = h->order.ensure(sizeof(int32_t) * (size_t)n)) != cudaSuccess)
+            return sfail(h, TAL_ENOMEM, "work order");
+        int32_t *order = reinterpret_cast<int32_t *>(h->order.p);
+        const int gb = (int)std::min<long long>(((long long)n + 255) / 256, 4LL * h->num_sms);
+        talsw::sw_bucket_count<<<gb, 256, 0, h->stream>>>(A.pairs, n, c->hist);
+        talsw::sw_bucket_offsets<<<1, 32, 0, h->stream>>>(c->hist);
+        talsw::sw_bucket_scatter<<<gb, 256, 0, h->stream>>>(A.pairs, n, c->hist, order);
+        if ((e = cudaGetLastError()) != cudaSuccess) return sfail(h, TAL_ECUDA, cudaGetErrorString(e));
+        A.order = order;
+    }
     A.work_counter = &c->counter;
     A.cells = &c->cells;
     A.err_flags = &c->flags;
     A.err_index = &c->bad;
-    const size_t wbytes = talsw::sw_warp_smem_bytes(A.cols_cap);
+    // 8- and 16-bit values fit int16: two pairs per warp in 16x2 lanes (the
+    // mismatch step, match - mismatch, must fit too)
+    const bool packed = bits != 32 && (long long)p.w_match - p.w_mismatch <= 32768;
+    const size_t wbytes = packed ? talsw::sw2_warp_smem_bytes(A.cols_cap)
+                                 : talsw::sw_warp_smem_bytes(A.cols_cap);
     const int wpb = 4;
     const size_t smem = wbytes * wpb;
     if (smem > h->smem_optin) return sfail(h, TAL_EDOMAIN, "sequences too long for shared memory");
     int bps = 0;
-    auto kern = talsw::sw_wave_kernel<talsw::kSwRows>;
+    auto kern = packed ? talsw::sw_wave2_kernel<talsw::kSwRows> : talsw::sw_wave_kernel<talsw::kSwRows>;
     e = talbsw::resident_blocks((const void *)kern, 32 * wpb, smem, h->smem_optin, &bps);
     if (e != cudaSuccess || bps < 1) return sfail(h, TAL_ECUDA, "occupancy query");
     long long blocks = (long long)bps * h->num_sms;
-    blocks = std::min<long long>(blocks, ((long long)n + wpb - 1) / wpb);
+    const long long pairs_per_block = (long long)wpb * (packed ? 2 : 1);
+    blocks = std::min<long long>(blocks, ((long long)n + pairs_per_block - 1) / pairs_per_block);
     kern<<<(unsigned)std::max<long long>(blocks, 1), 32 * wpb, smem, h->stream>>>(A);
     if ((e = cudaGetLastError()) != cudaSuccess) return sfail(h, TAL_ECUDA, cudaGetErrorString(e));
     SwCtrl out;
@@ -141,6 +163,7 @@ int tal_sw_destroy(tal_sw_handle h) {
         h->pairs.release();
         h->seq.release();
         h->ctrl.release();
+        h->order.release();
         cudaStreamDestroy(h->stream);
     }
     delete h;
