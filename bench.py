@@ -61,6 +61,9 @@ def parse_args():
                     help="pairs of the mixed-length workload (default: all 10,000,000)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
     ap.add_argument("--no-full-sw", action="store_true", help="skip the unbanded Smith-Waterman section")
+    ap.add_argument("--no-chain", action="store_true", help="skip the anchor chaining section")
+    ap.add_argument("--chain-reads", type=int, default=10_000,
+                    help="reads (1-10 kb, minimap2-like anchors) in the chaining section")
     ap.add_argument("--sw-pairs", type=int, default=100_000,
                     help="pairs of the unbanded Smith-Waterman workload")
     ap.add_argument("--serve-loads", type=float, nargs="+", default=[0.1, 0.3, 0.5, 0.7, 0.9])
@@ -427,6 +430,9 @@ def run_ours(args):
     if not args.no_full_sw:
         log("unbanded Smith-Waterman")
         result["full_sw"] = run_full_sw(args, dist)
+    if not args.no_chain:
+        log("anchor chaining")
+        result["chain"] = run_chain(args, dist)
     if not args.no_serving:
         log("serving loop")
         peak = result.get("mixed", {}).get("batched", {}).get("pairs_per_s")
@@ -722,6 +728,84 @@ def run_full_sw(args, dist):
         out["cpu_baseline"] = {"value": round(sample_cells / dt / 1e9, 4), "unit": "GCUPS", "cores": nth,
                                "kind": "port", "sample": f"first {k} pairs, oracle restatement"}
         out["outputs_match_oracle_sample"] = bool((exp["score"] == hpairs["score"][:k]).all())
+    return out
+
+
+def run_chain(args, dist):
+    """The anchor chaining DP (dp_chain::mm_dp_vectorized drop-in, the
+    reference driver's parameters): predecessor evaluations (the sum over
+    anchors of i - st, the reference loop's iterations) and anchors per second,
+    device-resident and end to end through mm_dp_batch on pinned host buffers."""
+    import torch
+    from tal_bsw import chaindata
+    from tal_bsw.chain import dp_chain
+    b = chaindata.generate(args.chain_reads, 1000, 10000, seed=77 + dist.rank)
+    P, dr, dq = chaindata.DRIVER_PARAMS, chaindata.DRIVER_DR, chaindata.DRIVER_DQ
+    n = b.n
+    out = {"workload": f"{b.n_reads} reads of U[1000,10000] bases, {n} anchors (span 15, one per "
+                       "1-10 query bases on the true diagonal, indel drift, 30% reads with a "
+                       "competing copy, 20% noise anchors), dp_chain(5000, 5000, 500, 25, 5000, "
+                       "1.0, 0, 1), dr = dq = 5000"}
+    with dp_chain(*P, device=dist.local) as ch:
+        stream = torch.cuda.ExternalStream(ch.stream)
+        da = torch.from_numpy(b.anchors.view(np.uint8).copy()).cuda()
+        do = torch.from_numpy(b.offsets.copy()).cuda()
+        df = torch.zeros(n, dtype=torch.int32, device="cuda")
+        dp_ = torch.zeros(n, dtype=torch.int32, device="cuda")
+        dv = torch.zeros(n, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+
+        def step():
+            ch.mm_dp_device(da.data_ptr(), do.data_ptr(), b.n_reads, dr, dq, df.data_ptr(),
+                            dp_.data_ptr(), dv.data_ptr())
+        for _ in range(3):
+            step()
+        evals = ch.last_evals
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        steps = 3
+        dist.barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = dist.max(e0.elapsed_time(e1) / 1e3 / steps)
+        out["device"] = {"evals_per_s": round(dist.sum(evals) / t, 1),
+                         "anchors_per_s": round(dist.sum(n) / t, 1), "ms_per_step": round(t * 1e3, 3),
+                         "evals_per_step": int(evals)}
+        ha = torch.empty(b.anchors.nbytes, dtype=torch.uint8, pin_memory=True)
+        ha.numpy()[:] = b.anchors.view(np.uint8)
+        anchors_pinned = ha.numpy().view(chaindata.ANCHOR_DTYPE)
+        ch.mm_dp_batch(anchors_pinned, b.offsets, dr, dq)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            gf, gp, gv = ch.mm_dp_batch(anchors_pinned, b.offsets, dr, dq)
+        te = dist.max((time.perf_counter() - t0) / steps)
+        out["e2e"] = {"evals_per_s": round(dist.sum(evals) / te, 1),
+                      "anchors_per_s": round(dist.sum(n) / te, 1), "ms_per_step": round(te * 1e3, 3),
+                      "h2d_bytes_per_step": int(b.anchors.nbytes + b.offsets.nbytes),
+                      "d2h_bytes_per_step": int(12 * n)}
+        out["outputs_match_device_path"] = bool(
+            (df.cpu().numpy().view(np.uint32) == gf).all() and (dp_.cpu().numpy() == gp).all()
+            and (dv.cpu().numpy() == gv).all())
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        import oracle
+        k = min(b.n_reads, 400)
+        sub_o = b.offsets[:k + 1]
+        sub_a = b.anchors[:int(sub_o[-1])]
+        nth = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ef, ep, ev = oracle.chain(sub_a, sub_o, P[2], P[4], dr, dq, nthreads=nth)
+        dt = time.perf_counter() - t0
+        # the sample's evaluations: i - st per anchor, from the same window rule
+        with dp_chain(*P, device=dist.local) as ch2:
+            sf, sp, sv = ch2.mm_dp_batch(sub_a, sub_o, dr, dq)
+            sample_evals = ch2.last_evals
+        out["cpu_baseline"] = {"evals_per_s": round(sample_evals / dt, 1), "cores": nth, "kind": "port",
+                               "sample": f"first {k} reads ({sub_a.shape[0]} anchors), oracle restatement"}
+        out["outputs_match_oracle_sample"] = bool((sf == ef).all() and (sp == ep).all() and (sv == ev).all())
     return out
 
 

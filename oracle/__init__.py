@@ -23,7 +23,7 @@ _PARAM_KEYS = ("o_del", "e_del", "o_ins", "e_ins", "zdrop", "end_bonus", "a", "b
 _libs: Dict[str, ctypes.CDLL] = {}
 
 
-ORACLE_SRCS = ("bsw_oracle.cpp", "sw_oracle.cpp")
+ORACLE_SRCS = ("bsw_oracle.cpp", "sw_oracle.cpp", "chain_oracle.cpp")
 
 
 def build(force: bool = False) -> str:
@@ -32,7 +32,8 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(ORACLE_SO) or \
             os.path.getmtime(ORACLE_SO) < max(os.path.getmtime(f) for f in srcs):
         os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
-        subprocess.check_call(["g++", "-O3", "-fPIC", "-shared", "-pthread", "-o", ORACLE_SO, *srcs])
+        subprocess.check_call(["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+                               "-pthread", "-o", ORACLE_SO, *srcs])
     return ORACLE_SO
 
 
@@ -225,3 +226,62 @@ def sw_reference(pairs: np.ndarray, seqbuf: np.ndarray, params: Dict[str, int],
 def sw_ref_max_len(bits: int) -> int:
     """The reference's MAX_SEQ_LEN for a precision (its sequence stride)."""
     return int(_sw_ref_lib().ref_sw_max_len(int(bits)))
+
+
+# ---------------------------------------------------------------- DP chaining
+ANCHOR_DTYPE = np.dtype([("r", "<u8"), ("q", "<i4"), ("l", "<i4")])
+CHAIN_REF_VARIANTS = ("avx512", "avx512_ofast", "avx2")
+
+
+def chain(anchors: np.ndarray, offsets: np.ndarray, bw: int, max_iter: int, dr: int, dq: int,
+          nthreads: int = 1):
+    """The reference's DP chaining (dp_chain::mm_dp_vectorized) restated
+    (oracle/chain_oracle.cpp); returns (f uint32, p int32, v int32)."""
+    a = np.ascontiguousarray(anchors, ANCHOR_DTYPE)
+    o = np.ascontiguousarray(offsets, np.int64)
+    n = a.shape[0]
+    f = np.zeros(n, np.uint32)
+    p = np.zeros(n, np.int32)
+    v = np.zeros(n, np.int32)
+    lib = _oracle()
+    lib.oracle_chain.restype = ctypes.c_int
+    lib.oracle_chain.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32] + \
+        [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 3 + [ctypes.c_int]
+    rc = lib.oracle_chain(_ptr(a), _ptr(o), o.shape[0] - 1, int(bw), int(max_iter), int(dr), int(dq),
+                          _ptr(f), _ptr(p), _ptr(v), int(nthreads))
+    if rc != 0:
+        raise ValueError("oracle_chain rejected its offsets")
+    return f, p, v
+
+
+def chain_ref_available(variant: str = "avx512") -> bool:
+    return os.path.exists(os.path.join(REF_DIR, f"libchain_ref_{variant}.so"))
+
+
+def chain_reference(anchors: np.ndarray, offsets: np.ndarray, params, dr: int, dq: int,
+                    variant: str = "avx512"):
+    """The reference's own dp_chain (built from its header by build_ref.sh;
+    variant: avx512, avx512_ofast or avx2); params: the constructor's eight
+    tunables in order.  Returns (f, p, v)."""
+    key = "chain_" + variant
+    if key not in _libs:
+        lib = ctypes.CDLL(os.path.join(REF_DIR, f"libchain_ref_{variant}.so"))
+        lib.ref_chain_run.restype = ctypes.c_int
+        lib.ref_chain_run.argtypes = [ctypes.c_int] * 5 + [ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                                           ctypes.c_void_p, ctypes.c_void_p,
+                                                           ctypes.c_int32, ctypes.c_int32,
+                                                           ctypes.c_int32] + [ctypes.c_void_p] * 3
+        _libs[key] = lib
+    a = np.ascontiguousarray(anchors, ANCHOR_DTYPE)
+    o = np.ascontiguousarray(offsets, np.int64)
+    n = a.shape[0]
+    f = np.zeros(n, np.uint32)
+    p = np.zeros(n, np.int32)
+    v = np.zeros(n, np.int32)
+    mdx, mdy, bw, msk, mit, gs, cdna, nseg = params
+    rc = _libs[key].ref_chain_run(int(mdx), int(mdy), int(bw), int(msk), int(mit), float(gs),
+                                  int(cdna), int(nseg), _ptr(a), _ptr(o), o.shape[0] - 1, int(dr),
+                                  int(dq), _ptr(f), _ptr(p), _ptr(v))
+    if rc != 0:
+        raise RuntimeError("ref_chain_run failed")
+    return f, p, v

@@ -43,5 +43,21 @@ if [ -f "$REF_SW/PairWiseSW_16.cpp" ] && grep -q avx512bw /proc/cpuinfo; then
   g++ -O2 -fPIC -shared -mavx512bw -fopenmp -w -I"$REF_SW" "$OUT"/sw_wrap/*.cpp \
       "$HERE/ref_sw_shim.cpp" -o "$OUT/libsw_ref_avx512.so" &
 fi
+
+# The DP chaining (src/chaining/parallel_chaining_32_bit.h), header only: the
+# AVX-512 path (the one benchmarks/bench-dp-chaining.cpp runs on an AVX-512
+# host), the same under the reference Makefile's -Ofast (fast-math may
+# reassociate the scalar path's double product), and the AVX2 path.
+REF_CH="${TAL_REFERENCE_ROOT:-/root/reference}/src/chaining"
+if [ -f "$REF_CH/parallel_chaining_32_bit.h" ]; then
+  chain() {  # $1 = flags, $2 = suffix
+    g++ -fPIC -shared $1 -w -I"$REF_CH" "$HERE/ref_chain_shim.cpp" -o "$OUT/libchain_ref_$2.so"
+  }
+  if grep -q avx512cd /proc/cpuinfo; then
+    chain "-O2 -mavx512f -mavx512bw -mavx512cd -mavx512vl" avx512 &
+    chain "-Ofast -mavx512f -mavx512bw -mavx512cd -mavx512vl" avx512_ofast &
+  fi
+  chain "-O2 -mavx2" avx2 &
+fi
 wait
 ls "$OUT"/*.so

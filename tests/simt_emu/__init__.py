@@ -118,3 +118,24 @@ def run_sw(pairs, seqbuf, stride, params, bits=16, warps=2, packed=None, order=N
                             vp(ordv.ctypes.data) if ordv is not None else None,
                             ctypes.byref(bad))
     return out, flags, bad.value
+
+
+def run_chain(anchors, offsets, bw, max_iter, dr, dq, warps=2):
+    """The anchor chaining kernel, emulated; returns (f, p, v, flags, bad, evals)."""
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+    a = np.ascontiguousarray(anchors)
+    o = np.ascontiguousarray(offsets, np.int64)
+    n = a.shape[0]
+    f = np.zeros(n, np.uint32)
+    p = np.zeros(n, np.int32)
+    v = np.zeros(n, np.int32)
+    ev = ctypes.c_ulonglong(0)
+    bad = ctypes.c_longlong(0)
+    vp = ctypes.c_void_p
+    _lib.emu_chain_run.restype = ctypes.c_int
+    flags = _lib.emu_chain_run(vp(a.ctypes.data), vp(o.ctypes.data), int(o.shape[0] - 1), int(bw),
+                               int(max_iter), int(dr), int(dq), vp(f.ctypes.data), vp(p.ctypes.data),
+                               vp(v.ctypes.data), int(warps), ctypes.byref(ev), ctypes.byref(bad))
+    return f, p, v, flags, bad.value, ev.value

@@ -20,6 +20,7 @@ std::mutex atomic_mu;
 #include "bsw_kernel.cuh"
 #include "bsw_lane.cuh"
 #include "sw_kernel.cuh"
+#include "chain_kernel.cuh"
 #include <functional>
 
 // Runs one launch of A (one block of `warps` warps); -1 if a warp's lanes
@@ -29,8 +30,9 @@ std::mutex atomic_mu;
 static int sw_packed = 0;  // the unbanded kernel: 1 = two pairs per warp (16x2)
 
 static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
-                      const talsw::SwArgs *sw = nullptr) {
-    size_t wbytes = sw ? (sw_packed ? talsw::sw2_warp_smem_bytes(sw->cols_cap) : talsw::sw_warp_smem_bytes(sw->cols_cap))
+                      const talsw::SwArgs *sw = nullptr, const talchain::ChainArgs *ch = nullptr) {
+    size_t wbytes = ch ? 16
+                  : sw ? (sw_packed ? talsw::sw2_warp_smem_bytes(sw->cols_cap) : talsw::sw_warp_smem_bytes(sw->cols_cap))
                   : G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap, A.win)
                            : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G, A.win);
     std::vector<unsigned char> smem(wbytes * warps + 64, 0xA5);  // poisoned, like fresh smem
@@ -39,10 +41,10 @@ static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
     for (int wi = 0; wi < warps; wi++) {
         simt::Warp *W = new simt::Warp();
         std::vector<std::vector<char>> stacks(32, std::vector<char>(1 << 18));
-        struct Arg { int t; simt::Warp *W; const talbsw::LaunchArgs *A; int G, K; unsigned char *sm; int warps; const talsw::SwArgs *sw; };
+        struct Arg { int t; simt::Warp *W; const talbsw::LaunchArgs *A; int G, K; unsigned char *sm; int warps; const talsw::SwArgs *sw; const talchain::ChainArgs *ch; };
         static thread_local Arg args[32];
         for (int l = 0; l < 32; l++) {
-            args[l] = Arg{wi * 32 + l, W, &A, G, K, smem.data(), warps, sw};
+            args[l] = Arg{wi * 32 + l, W, &A, G, K, smem.data(), warps, sw, ch};
             getcontext(&W->lane_ctx[l]);
             W->lane_ctx[l].uc_stack.ss_sp = stacks[l].data();
             W->lane_ctx[l].uc_stack.ss_size = stacks[l].size();
@@ -55,6 +57,7 @@ static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
                 simt::tl_gridDim.x = 1;
                 simt::tl_warp = a.W;
                 simt::tl_smem = a.sm;
+                if (a.ch) { talchain::chain_kernel(*a.ch); a.W->done[a.t & 31] = true; return; }
                 if (a.sw) { if (sw_packed) talsw::sw_wave2_kernel<talsw::kSwRows>(*a.sw); else talsw::sw_wave_kernel<talsw::kSwRows>(*a.sw); a.W->done[a.t & 31] = true; return; }
                 if (a.G == 1) { const bool sym = a.A->P.o_del == a.A->P.o_ins && a.A->P.e_del == a.A->P.e_ins; int v = a.K == 4 ? 3 : a.K == 2 ? 2 : 1; if (!sym) v &= 1; if (v == 3) talbsw::bsw_lane_kernel<3>(*a.A); else if (v == 2) talbsw::bsw_lane_kernel<2>(*a.A); else if (v == 1) talbsw::bsw_lane_kernel<1>(*a.A); else talbsw::bsw_lane_kernel<0>(*a.A); a.W->done[a.t & 31] = true; return; }
                 switch (a.G * 10 + a.K) {
@@ -181,6 +184,33 @@ extern "C" int emu_sw_run(void *pairs, int n, const uint8_t *seqbuf, long long s
     talbsw::LaunchArgs A;
     std::memset(&A, 0, sizeof(A));
     const int rc = run_launch(A, 1, 4, warps, &S);
+    *bad = badi;
+    return rc < 0 ? -1 : flags;
+}
+
+
+// The anchor chaining kernel over n_reads reads (anchors 16-byte records, read
+// k = [offsets[k], offsets[k+1])).  Returns the kernel's error flags (first
+// bad read in *bad), -1 on a divergent exit.
+extern "C" int emu_chain_run(const void *anchors, const int64_t *offsets, int n_reads, int bw,
+                             int max_iter, int dr, int dq, uint32_t *f, int32_t *p, int32_t *v,
+                             int warps, unsigned long long *evals, long long *bad) {
+    talchain::ChainArgs C;
+    std::memset(&C, 0, sizeof(C));
+    C.anchors = static_cast<const talchain::Anchor *>(anchors);
+    C.offsets = offsets;
+    C.n_reads = n_reads;
+    C.bw = bw; C.max_iter = max_iter; C.dr = dr; C.dq = dq;
+    std::vector<int2> rq((size_t)std::max<int64_t>(offsets[n_reads], 1));
+    C.rq = rq.data();
+    C.f = f; C.p = p; C.v = v;
+    int counter = 0, flags = 0;
+    long long badi = (long long)INT64_MAX;
+    *evals = 0;
+    C.work_counter = &counter; C.evals = evals; C.err_flags = &flags; C.err_index = &badi;
+    talbsw::LaunchArgs A;
+    std::memset(&A, 0, sizeof(A));
+    const int rc = run_launch(A, 1, 4, warps, nullptr, &C);
     *bad = badi;
     return rc < 0 ? -1 : flags;
 }

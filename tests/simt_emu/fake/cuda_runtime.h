@@ -5,6 +5,7 @@
 #pragma once
 #include <atomic>
 #include <climits>
+#include <cmath>
 #include <cstdlib>
 #include <ucontext.h>
 #include <cstdint>
@@ -157,6 +158,25 @@ inline int __viaddmax_s32(int a, int b, int c) { int s = a + b; return s > c ? s
 inline int __viaddmax_s32_relu(int a, int b, int c) { int s = a + b; int m = s > c ? s : c; return m > 0 ? m : 0; }
 inline int __vimax3_s32(int a, int b, int c) { int m = a > b ? a : b; return m > c ? m : c; }
 inline int __vimax3_s32_relu(int a, int b, int c) { int m = __vimax3_s32(a, b, c); return m > 0 ? m : 0; }
+// Rounded conversions and products as the device intrinsics define them (the
+// host computes in IEEE single / double with round-to-nearest, no contraction
+// in a single product).
+inline float __fmul_rn(float a, float b) { volatile float r = a * b; return r; }
+inline float __fdiv_rn(float a, float b) { volatile float r = a / b; return r; }
+inline double __dmul_rn(double a, double b) { volatile double r = a * b; return r; }
+inline float __int2float_rn(int x) { return (float)x; }
+inline float __ull2float_rn(unsigned long long x) { return (float)x; }
+inline float __ll2float_rn(long long x) { return (float)x; }
+inline float __double2float_rn(double x) { return (float)x; }
+inline int __float2int_rd(float x) {  // saturating, like the device conversion
+    const double d = std::floor((double)x);
+    return d >= 2147483647.0 ? INT_MAX : d <= -2147483648.0 ? INT_MIN : (int)d;
+}
+inline int __double2int_rz(double x) {
+    const double d = std::trunc(x);
+    return d >= 2147483647.0 ? INT_MAX : d <= -2147483648.0 ? INT_MIN : (int)d;
+}
+
 // 16x2 forms: each 16-bit half on its own
 inline int sw_lo16(unsigned v) { return (int)(short)(v & 0xffffu); }
 inline int sw_hi16(unsigned v) { return (int)(short)(v >> 16); }

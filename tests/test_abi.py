@@ -75,11 +75,20 @@ def test_ctypes_structs_match_the_header(tmp_path):
         _fields_ = [(n, {"<i4": ctypes.c_int32, "<i2": ctypes.c_int16}[SW_DTYPE.fields[n][0].str])
                     for n in SW_DTYPE.names]
         _pack_ = 1
+    from tal_bsw.chain import _ChainParams
+    from tal_bsw.chaindata import ANCHOR_DTYPE
+
+    class _Anchor(ctypes.Structure):
+        _fields_ = [("r", ctypes.c_uint64), ("q", ctypes.c_int32), ("l", ctypes.c_int32)]
+    assert ctypes.sizeof(_Anchor) == ANCHOR_DTYPE.itemsize
+    assert [ANCHOR_DTYPE.fields[n][1] for n in ANCHOR_DTYPE.names] == \
+        [getattr(_Anchor, n).offset for n, _ in _Anchor._fields_]
     structs = {"tal_bsw_server_config": ServerConfig, "tal_bsw_request_info": RequestInfo,
                "tal_bsw_server_stats": ServerStats, "tal_bsw_params": _Params,
-               "tal_sw_params": _SwParams, "tal_sw_pair": _SwPair}
+               "tal_sw_params": _SwParams, "tal_sw_pair": _SwPair,
+               "tal_chain_params": _ChainParams, "tal_anchor": _Anchor}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "tal_bsw.h"', '#include "tal_sw.h"',
-             "int main(void) {"]
+             '#include "tal_chain.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
         for f, _ in py._fields_:

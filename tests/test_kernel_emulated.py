@@ -232,3 +232,54 @@ def test_emulated_sw_two_pairs_per_warp_bad_pair():
                                       order=np.array([5, 3, 0, 1, 2, 4], np.int32))
     assert flags != 0 and bad == 3
     assert (got["score"][[0, 1, 2, 4, 5]] == exp["score"]).all()
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLDEN, "chain", "*.npz"))), ids=os.path.basename)
+def test_emulated_chain_kernel_matches_golden(f):
+    """The anchor chaining kernel (one warp per read, lanes over the
+    predecessors, two warp reductions per anchor) against the reference's
+    outputs; reads cut to keep the emulation short."""
+    d = np.load(f)
+    P = [float(x) for x in d["params"]]
+    offs = d["offsets"]
+    keep = min(offs.shape[0] - 1, 6)
+    end = int(offs[keep])
+    # at most 600 anchors per read: the first anchors of a read do not depend on later ones
+    a_parts, o_new, idx = [], [0], []
+    for k in range(keep):
+        lo, hi = int(offs[k]), int(min(offs[k + 1], offs[k] + 600))
+        idx.extend(range(lo, hi))
+        o_new.append(o_new[-1] + hi - lo)
+    idx = np.array(idx, np.int64)
+    anchors = d["anchors"][idx]
+    offsets = np.array(o_new, np.int64)
+    # the cut changes avg_l, so the expectation is the oracle's on the cut reads,
+    # itself pinned to the reference on the full fixtures
+    ef, ep, ev = oracle.chain(anchors, offsets, int(P[2]), int(P[4]), int(d["dr"]), int(d["dq"]))
+    gf, gp, gv, flags, _, evals = simt_emu.run_chain(anchors, offsets, int(P[2]), int(P[4]),
+                                                     int(d["dr"]), int(d["dq"]), warps=2)
+    assert flags == 0
+    assert (gf == ef).all() and (gp == ep).all() and (gv == ev).all()
+    assert end >= 0 and evals > 0
+
+
+def test_emulated_chain_kernel_full_fixture_short_reads():
+    """Whole fixture (no cut) where it is small: the reference's own outputs."""
+    d = np.load(os.path.join(GOLDEN, "chain", "short_reads.npz"))
+    P = [float(x) for x in d["params"]]
+    gf, gp, gv, flags, _, _ = simt_emu.run_chain(d["anchors"], d["offsets"], int(P[2]), int(P[4]),
+                                                 int(d["dr"]), int(d["dq"]), warps=2)
+    assert flags == 0
+    assert (gf == d["f"]).all() and (gp == d["p"]).all() and (gv == d["v"]).all()
+
+
+def test_emulated_chain_kernel_rejects_negative_length():
+    from tal_bsw import chaindata
+    a = np.zeros(5, chaindata.ANCHOR_DTYPE)
+    a["r"] = np.arange(5) * 10
+    a["q"] = np.arange(5) * 10
+    a["l"] = [15, 15, -1, 15, 15]
+    offs = np.array([0, 2, 5], np.int64)
+    gf, gp, gv, flags, bad, _ = simt_emu.run_chain(a, offs, 500, 5000, 5000, 5000)
+    assert flags != 0 and bad == 1
+    assert gf[:2].tolist() == [15, 25]
