@@ -31,7 +31,7 @@ static int sw_packed = 0;  // the unbanded kernel: 1 = two pairs per warp (16x2)
 
 static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
                       const talsw::SwArgs *sw = nullptr, const talchain::ChainArgs *ch = nullptr) {
-    size_t wbytes = ch ? 16
+    size_t wbytes = ch ? talchain::chain_warp_smem_bytes(ch->bw) + 16
                   : sw ? (sw_packed ? talsw::sw2_warp_smem_bytes(sw->cols_cap) : talsw::sw_warp_smem_bytes(sw->cols_cap))
                   : G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap, A.win)
                            : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G, A.win);

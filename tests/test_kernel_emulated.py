@@ -283,3 +283,18 @@ def test_emulated_chain_kernel_rejects_negative_length():
     gf, gp, gv, flags, bad, _ = simt_emu.run_chain(a, offs, 500, 5000, 5000, 5000)
     assert flags != 0 and bad == 1
     assert gf[:2].tolist() == [15, 25]
+
+
+def test_emulated_chain_kernel_windows_past_the_ring():
+    """Dense anchors (one per base or two): predecessor windows of over a
+    thousand anchors, so part of each window comes from global memory instead
+    of the warp's shared-memory ring of the newest 1,024."""
+    from tal_bsw import chaindata
+    b = chaindata.generate(2, 2600, 2800, seed=21, spacing=2, noise=0.0, repeat=0.0)
+    n0 = int(b.offsets[1] - b.offsets[0])
+    P = chaindata.DRIVER_PARAMS
+    ef, ep, ev = oracle.chain(b.anchors, b.offsets, P[2], P[4], 5000, 5000)
+    gf, gp, gv, flags, _, evals = simt_emu.run_chain(b.anchors, b.offsets, P[2], P[4], 5000, 5000, warps=2)
+    assert flags == 0 and n0 > 2000
+    assert evals > 1100 * n0  # windows wider than the ring
+    assert (gf == ef).all() and (gp == ep).all() and (gv == ev).all()

@@ -21,7 +21,7 @@ static_assert(sizeof(talchain::Anchor) == 16, "device view");
 
 namespace {
 
-constexpr int kBlocksPerSm = 4;
+constexpr int kBlocksPerSm = 8;
 
 struct ChainCtrl {
     int counter;
@@ -92,12 +92,15 @@ int run_locked(tal_chain_ctx *h, const tal_anchor *d_anchors, const int64_t *d_o
     A.err_flags = &c->flags;
     A.err_index = &c->bad;
     const int wpb = 4;
+    const size_t smem = wpb * talchain::chain_warp_smem_bytes(A.bw);  // rings and gap tables
+    e = cudaFuncSetAttribute(talchain::chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cfail(h, TAL_ECUDA, "shared memory opt-in");
     int bps = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, talchain::chain_kernel, 32 * wpb, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, talchain::chain_kernel, 32 * wpb, smem);
     if (e != cudaSuccess || bps < 1) return cfail(h, TAL_ECUDA, "occupancy query");
     long long blocks = (long long)std::min(bps, blocks_per_sm()) * h->num_sms;
     blocks = std::min<long long>(blocks, ((long long)n_reads + wpb - 1) / wpb);
-    talchain::chain_kernel<<<(unsigned)std::max<long long>(blocks, 1), 32 * wpb, 0, h->stream>>>(A);
+    talchain::chain_kernel<<<(unsigned)std::max<long long>(blocks, 1), 32 * wpb, smem, h->stream>>>(A);
     if ((e = cudaGetLastError()) != cudaSuccess) return cfail(h, TAL_ECUDA, cudaGetErrorString(e));
     ChainCtrl out;
     e = cudaMemcpyAsync(&out, c, sizeof(out), cudaMemcpyDeviceToHost, h->stream);
