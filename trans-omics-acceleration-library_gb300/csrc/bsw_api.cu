@@ -12,6 +12,7 @@
 #include <string>
 
 #include "bsw_ctx.h"
+#include "bucket_scan.cuh"
 
 static_assert(sizeof(tal_seq_pair) == 56, "SeqPair is 14 x int32 (bandedSWA.h:90-99)");
 static_assert(sizeof(talbsw::DevPair) == 56, "device SeqPair view");
@@ -37,6 +38,52 @@ struct Ctrl {
     unsigned long long cells;
 };
 
+// Work order of a plain launch: the reference sorts each thread's pairs by
+// target length before scoring them (sortPairsLen, bandedSWA.cpp:1909-1950,
+// called at :2742 and :2046) so that a SIMD group's pairs end together; here
+// the order groups pairs of about the same target length (buckets of four
+// bases, longest first) into the same warp.  Outputs do not depend on it.
+constexpr int kOrderMin = 2048;  // smaller batches keep their order
+
+__device__ __forceinline__ int plain_bucket(const talbsw::DevPair &p) {
+    int b = p.len1 < 0 ? 0 : p.len1 >> 2;
+    b = b > talbsw::kScanBuckets - 1 ? talbsw::kScanBuckets - 1 : b;
+    return (talbsw::kScanBuckets - 1) - b;
+}
+
+__global__ void plain_count(const talbsw::DevPair *pairs, int n, int *hist) {
+    __shared__ int sh[talbsw::kScanBuckets];
+    for (int t = threadIdx.x; t < talbsw::kScanBuckets; t += blockDim.x) sh[t] = 0;
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&sh[plain_bucket(pairs[i])], 1);
+    __syncthreads();
+    for (int t = threadIdx.x; t < talbsw::kScanBuckets; t += blockDim.x)
+        if (sh[t]) atomicAdd(&hist[t], sh[t]);
+}
+
+__global__ void plain_scatter(const talbsw::DevPair *pairs, int n, int *offs, int32_t *order) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        order[atomicAdd(&offs[plain_bucket(pairs[i])], 1)] = i;
+}
+
+cudaError_t enqueue_plain_order(tal_bsw_ctx *h, talbsw::LaunchArgs &A) {
+    const size_t hb = sizeof(int) * talbsw::kScanBuckets;
+    cudaError_t e = h->porder.ensure(4 * (size_t)A.n + hb);
+    if (e != cudaSuccess) return e;
+    int32_t *order = reinterpret_cast<int32_t *>(h->porder.p);
+    int *hist = reinterpret_cast<int *>(order + A.n);
+    if ((e = cudaMemsetAsync(hist, 0, hb, h->stream)) != cudaSuccess) return e;
+    const int gb = (int)std::min<long long>(((long long)A.n + 255) / 256, 2LL * h->num_sms);
+    plain_count<<<gb, 256, 0, h->stream>>>(A.pairs, A.n, hist);
+    talbsw::bucket_scan_4096<<<1, 1024, 0, h->stream>>>(hist);
+    plain_scatter<<<gb, 256, 0, h->stream>>>(A.pairs, A.n, hist, order);
+    h->launches += 3;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    A.order = order;
+    return cudaSuccess;
+}
+
 // Issues the scoring launch for pairs already on the device.
 int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
     Ctrl *c = reinterpret_cast<Ctrl *>(h->ctrl.p);
@@ -54,6 +101,9 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
     Ctrl init = {0, 0, (long long)INT64_MAX, 0ull};
     cudaError_t e = cudaMemcpyAsync(c, &init, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(ctrl)");
+    if (A.order == nullptr && A.n >= kOrderMin && !getenv("TAL_BSW_NO_ORDER")) {
+        if ((e = enqueue_plain_order(h, A)) != cudaSuccess) return cuda_fail(h, e, "work order");
+    }
     e = talbsw::launch_config(A, cfg, h->num_sms, h->smem_optin, h->stream);
     h->launches++;
     if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
@@ -134,6 +184,7 @@ int tal_bsw_destroy(tal_bsw_handle h) {
         h->caps.release();
         h->bcounts.release();
         h->border.release();
+        h->porder.release();
         h->bseg.release();
         h->bctrl.release();
         h->btune_seg.release();

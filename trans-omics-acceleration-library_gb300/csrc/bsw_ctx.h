@@ -198,6 +198,7 @@ struct tal_bsw_ctx {
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
     talbsw::DevBuf pairs, ref, qer, ctrl, wpair, caps;
+    talbsw::DevBuf porder;  // plain launch: work order by target length, and its buckets
     // batched form
     talbsw::DevBuf bcounts, border, bseg, bctrl, btune_seg;
     talbsw::BinFork bfork;

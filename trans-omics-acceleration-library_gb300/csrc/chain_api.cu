@@ -242,7 +242,7 @@ int tal_chain_dp_device(tal_chain_handle h, const tal_anchor *d_anchors, const i
     if (e != cudaSuccess) return cfail(h, TAL_ECUDA, cudaGetErrorString(e));
     const int gb = (int)std::min<long long>(((long long)n_reads + 255) / 256, 4LL * h->num_sms);
     talchain::ch_bucket_count<<<gb, 256, 0, h->stream>>>(d_offsets, n_reads, hist);
-    talchain::ch_bucket_offsets<<<1, 1024, 0, h->stream>>>(hist);
+    talbsw::bucket_scan_4096<<<1, 1024, 0, h->stream>>>(hist);
     talchain::ch_bucket_scatter<<<gb, 256, 0, h->stream>>>(d_offsets, n_reads, hist, order);
     if ((e = cudaGetLastError()) != cudaSuccess) return cfail(h, TAL_ECUDA, cudaGetErrorString(e));
     return run_locked(h, d_anchors, d_offsets, order, n_reads, n_anchors, dr, dq, d_f, d_p, d_v);

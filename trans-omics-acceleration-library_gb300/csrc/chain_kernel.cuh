@@ -33,6 +33,8 @@
 
 #include <climits>
 
+#include "bucket_scan.cuh"
+
 #ifndef TALBSW_DYNAMIC_SMEM
 #define TALBSW_DYNAMIC_SMEM(name) extern __shared__ __align__(16) unsigned char name[]
 #endif
@@ -84,7 +86,7 @@ __device__ __forceinline__ int32_t ch_gap_double(int32_t dd, double avg) {
 
 // Read order for device-resident batches: by anchor count, longest first, in
 // buckets of 16 anchors (a counting sort), so no long read starts last.
-constexpr int kChainBuckets = 4096;  // = 4 x the 1024 threads of ch_bucket_offsets
+constexpr int kChainBuckets = talbsw::kScanBuckets;  // scanned by talbsw::bucket_scan_4096
 
 __device__ __forceinline__ int ch_bucket(const int64_t *offsets, int k) {
     int64_t n = offsets[k + 1] - offsets[k];
@@ -95,43 +97,6 @@ __device__ __forceinline__ int ch_bucket(const int64_t *offsets, int k) {
 __global__ void ch_bucket_count(const int64_t *offsets, int n_reads, int *hist) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_reads; k += gridDim.x * blockDim.x)
         atomicAdd(&hist[ch_bucket(offsets, k)], 1);
-}
-
-// Counts -> first positions (exclusive scan), one block of 1024 threads, four
-// buckets per thread.
-__global__ void __launch_bounds__(1024) ch_bucket_offsets(int *hist) {
-    __shared__ int wsum[32];
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    int c[4], run = 0;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        c[k] = hist[4 * t + k];
-        run += c[k];
-    }
-    int incl = run;  // inclusive scan of the per-thread sums over the warp
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += y;
-    }
-    if (lane == 31) wsum[w] = incl;
-    __syncthreads();
-    if (w == 0) {
-        int x = wsum[lane];
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, x, d);
-            if (lane >= d) x += y;
-        }
-        wsum[lane] = x;  // inclusive over warps
-    }
-    __syncthreads();
-    int pos = incl - run + (w > 0 ? wsum[w - 1] : 0);
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        hist[4 * t + k] = pos;
-        pos += c[k];
-    }
 }
 
 __global__ void ch_bucket_scatter(const int64_t *offsets, int n_reads, int *offs, int32_t *order) {
