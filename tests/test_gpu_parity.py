@@ -100,3 +100,69 @@ def test_out_of_range_rejected():
         assert ei.value.status == tal_bsw.api.TAL_EDOMAIN
         assert ei.value.bad_pair == 0
     assert (outputs(got) == -1).all(), "no outputs are written on a range error"
+
+
+@pytest.mark.parametrize("wl,bits", [(synth.C2, 16), (synth.C1_8, 8), (synth.C3, 0)])
+def test_plain_launch_length_order(wl, bits):
+    """Batches from 2,048 pairs run in target-length order (a device counting
+    sort before the scoring launch): the outputs equal the oracle's and those
+    of the caller's order (TAL_BSW_NO_ORDER), pair by pair."""
+    b = synth.generate(wl, 6000)
+    P = b.workload.params()
+    w = 100
+    exp = oracle.routed(b.pairs, b.ref, b.qer, w, P, bits=bits)
+    got = _gpu(b.pairs, b.ref, b.qer, w, P, bits)
+    _assert_same(exp, got, f"{wl.name} ordered")
+    os.environ["TAL_BSW_NO_ORDER"] = "1"
+    try:
+        unordered = _gpu(b.pairs, b.ref, b.qer, w, P, bits)
+    finally:
+        del os.environ["TAL_BSW_NO_ORDER"]
+    _assert_same(unordered, got, f"{wl.name} ordered vs caller's order")
+
+
+def test_plain_launch_length_order_reports_the_callers_index():
+    """A bad pair inside a length-ordered launch is reported by its index in
+    the caller's array."""
+    b = synth.generate(synth.C2, 5000)
+    P = b.workload.params()
+    q = b.qer.copy()
+    k = 3001
+    q[int(b.pairs["idq"][k]) + 3] = 9   # a query base code above 4
+    got = b.pairs.copy()
+    with _bsw(P) as bsw:
+        with pytest.raises(tal_bsw.TalBswError) as ei:
+            bsw.getScores16(got, b.ref, q, b.n, 1, 100)
+    assert ei.value.bad_pair == k
+
+
+def test_host_call_in_chunks():
+    """Host-buffer calls of 262,144+ pairs copy and score in four chunks (the
+    next chunk's copies overlap this chunk's scoring): outputs equal the
+    device-resident call's and, on a sample, the oracle's; a bad pair in a
+    later chunk is reported by its index in the caller's array."""
+    import torch
+    b = synth.generate(synth.C2, 300000)
+    P = b.workload.params()
+    got = b.pairs.copy()
+    with _bsw(P) as bsw:
+        bsw.getScores16(got, b.ref, b.qer, b.n, 1, 100)
+        dp = torch.from_numpy(b.pairs.view(np.uint8).reshape(-1).copy()).cuda()
+        dr = torch.from_numpy(b.ref).cuda()
+        dq = torch.from_numpy(b.qer).cuda()
+        bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(), b.n,
+                          100, 16)
+        bsw.sync()
+        dev = dp.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE)
+        _assert_same(dev, got, "chunked host call vs device-resident call")
+        k = np.arange(0, b.n, 150)
+        exp = oracle.vector(b.pairs[k], b.ref, b.qer, 100, P, bits=16)
+        _assert_same(exp, got[k], "chunked host call vs oracle (sample)")
+        q = b.qer.copy()
+        bad = 250001
+        q[int(b.pairs["idq"][bad]) + 2] = 7
+        g2 = b.pairs.copy()
+        with pytest.raises(tal_bsw.TalBswError) as ei:
+            bsw.getScores16(g2, b.ref, q, b.n, 1, 100)
+        assert ei.value.bad_pair == bad
+        assert (outputs(g2) == -1).all(), "no outputs are written on an error"

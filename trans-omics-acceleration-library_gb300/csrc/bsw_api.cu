@@ -10,6 +10,8 @@
 #include <climits>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "bsw_ctx.h"
 #include "bucket_scan.cuh"
@@ -84,9 +86,19 @@ cudaError_t enqueue_plain_order(tal_bsw_ctx *h, talbsw::LaunchArgs &A) {
     return cudaSuccess;
 }
 
-// Issues the scoring launch for pairs already on the device.
-int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
-    Ctrl *c = reinterpret_cast<Ctrl *>(h->ctrl.p);
+// Host-buffer calls from this many pairs copy and score in kChunks chunks
+// (chunk k + 1's copies overlap chunk k's scoring); each chunk has its own
+// control block.
+constexpr int kChunks = 4;
+constexpr int kChunkMin = 262144;
+
+int collect_chunks(tal_bsw_ctx *h, int nslots, int32_t per);
+int collect(tal_bsw_ctx *h) { return collect_chunks(h, 1, 0); }
+
+// Issues the scoring launch for pairs already on the device (control block
+// `slot`).
+int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k, int slot = 0) {
+    Ctrl *c = reinterpret_cast<Ctrl *>(h->ctrl.p) + slot;
     A.work_counter = &c->counter;
     A.err_flags = &c->flags;
     A.err_index = &c->bad_index;
@@ -110,11 +122,21 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k) {
     return TAL_OK;
 }
 
-int collect(tal_bsw_ctx *h) {
-    Ctrl c;
-    cudaError_t e = cudaMemcpyAsync(&c, h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream);
+// Waits for the launches of control blocks [0, nslots) and merges their
+// status: flags or-ed, the first bad pair (block k's pair indices start at
+// k * per), cells summed.
+int collect_chunks(tal_bsw_ctx *h, int nslots, int32_t per) {
+    Ctrl cs[kChunks];
+    cudaError_t e = cudaMemcpyAsync(cs, h->ctrl.p, sizeof(Ctrl) * nslots, cudaMemcpyDeviceToHost,
+                                    h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "scoring");
+    Ctrl c = {0, 0, (long long)INT64_MAX, 0ull};
+    for (int k = 0; k < nslots; k++) {
+        c.flags |= cs[k].flags;
+        if (cs[k].flags) c.bad_index = std::min(c.bad_index, (long long)k * per + cs[k].bad_index);
+        c.cells += cs[k].cells;
+    }
     h->last_cells = c.cells;
     if (c.flags) {
         h->last_bad = c.bad_index;
@@ -159,7 +181,7 @@ int tal_bsw_create(const tal_bsw_params *params, int device, tal_bsw_handle *out
     h->num_sms = prop.multiProcessorCount;
     h->smem_optin = prop.sharedMemPerBlockOptin;
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = h->ctrl.ensure(sizeof(Ctrl));
+    if (e == cudaSuccess) e = h->ctrl.ensure(sizeof(Ctrl) * kChunks);
     if (e != cudaSuccess) {
         if (h->stream) cudaStreamDestroy(h->stream);
         h->ctrl.release();
@@ -191,6 +213,9 @@ int tal_bsw_destroy(tal_bsw_handle h) {
         h->bfork.release();
         for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second.exec);
         h->graphs.clear();
+        for (cudaEvent_t &ev : h->cev)
+            if (ev) cudaEventDestroy(ev);
+        if (h->cstream) cudaStreamDestroy(h->cstream);
         cudaStreamDestroy(h->stream);
     }
     delete h;
@@ -209,58 +234,150 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
     if (!pairs || !seqBufRef || !seqBufQer) return fail(h, TAL_EINVAL, "NULL buffer");
     cudaError_t e = cudaSetDevice(h->device);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
-    // extents of the byte windows the pairs reference, and row capacities
-    long long rlo = LLONG_MAX, rhi = 0, qlo = LLONG_MAX, qhi = 0;
-    int max1 = 0, max2 = 0;
-    for (int32_t k = 0; k < numPairs; k++) {
-        const tal_seq_pair &p = pairs[k];
-        if (p.len1 < 0 || p.len2 < 0 || p.idr < 0 || p.idq < 0) {
-            h->last_bad = k;
-            return fail(h, TAL_EDOMAIN, "negative length or offset at pair " + std::to_string(k));
-        }
-        rlo = std::min<long long>(rlo, p.idr);
-        qlo = std::min<long long>(qlo, p.idq);
-        rhi = std::max<long long>(rhi, (long long)p.idr + p.len1);
-        qhi = std::max<long long>(qhi, (long long)p.idq + p.len2);
-        max1 = std::max(max1, p.len1);
-        max2 = std::max(max2, p.len2);
+    // Per chunk of pairs: the byte windows they reference and their row
+    // capacities (one host thread per chunk)
+    struct Ext {
+        long long rlo = LLONG_MAX, rhi = 0, qlo = LLONG_MAX, qhi = 0;
+        int max1 = 0, max2 = 0;
+        int32_t bad = -1;
+    };
+    int nch = numPairs >= kChunkMin ? kChunks : 1;
+    if (const char *ev = getenv("TAL_BSW_CHUNKS")) {  // tuning: 1 .. kChunks
+        const int c = atoi(ev);
+        if (c >= 1 && c <= kChunks) nch = numPairs >= kChunkMin ? c : 1;
     }
-    rlo &= ~15LL;
-    qlo &= ~15LL;
-    if (rhi <= rlo) rhi = rlo + 16;
-    if (qhi <= qlo) qhi = qlo + 16;
+    int32_t per = (numPairs + nch - 1) / nch;
+    Ext ext[kChunks];
+    auto scan = [&](int c) {
+        Ext &x = ext[c];
+        const int32_t k1 = std::min<int32_t>(numPairs, (c + 1) * per);
+        for (int32_t k = c * per; k < k1; k++) {
+            const tal_seq_pair &p = pairs[k];
+            if (p.len1 < 0 || p.len2 < 0 || p.idr < 0 || p.idq < 0) {
+                x.bad = k;
+                return;
+            }
+            x.rlo = std::min<long long>(x.rlo, p.idr);
+            x.qlo = std::min<long long>(x.qlo, p.idq);
+            x.rhi = std::max<long long>(x.rhi, (long long)p.idr + p.len1);
+            x.qhi = std::max<long long>(x.qhi, (long long)p.idq + p.len2);
+            x.max1 = std::max(x.max1, p.len1);
+            x.max2 = std::max(x.max2, p.len2);
+        }
+    };
+    if (nch > 1) {
+        std::vector<std::thread> th;
+        for (int c = 0; c < nch; c++) th.emplace_back(scan, c);
+        for (auto &t : th) t.join();
+    } else {
+        scan(0);
+    }
+    Ext all;
+    for (int c = 0; c < nch; c++) {
+        if (ext[c].bad >= 0) {
+            h->last_bad = ext[c].bad;
+            return fail(h, TAL_EDOMAIN, "negative length or offset at pair " + std::to_string(ext[c].bad));
+        }
+        if ((int64_t)c * per >= numPairs) continue;
+        all.rlo = std::min(all.rlo, ext[c].rlo);
+        all.qlo = std::min(all.qlo, ext[c].qlo);
+        all.rhi = std::max(all.rhi, ext[c].rhi);
+        all.qhi = std::max(all.qhi, ext[c].qhi);
+        all.max1 = std::max(all.max1, ext[c].max1);
+        all.max2 = std::max(all.max2, ext[c].max2);
+    }
+    auto align = [](Ext &x) {
+        x.rlo &= ~15LL;
+        x.qlo &= ~15LL;
+        if (x.rhi <= x.rlo) x.rhi = x.rlo + 16;
+        if (x.qhi <= x.qlo) x.qhi = x.qlo + 16;
+    };
+    align(all);
+    for (int c = 0; c < nch; c++) align(ext[c]);
+    // chunk windows that overlap much (pairs sharing sequences) copy once, whole
+    long long sum = 0;
+    for (int c = 0; c < nch; c++) sum += (ext[c].rhi - ext[c].rlo) + (ext[c].qhi - ext[c].qlo);
+    if (nch > 1 && sum * 4 > ((all.rhi - all.rlo) + (all.qhi - all.qlo)) * 5) nch = 1;
+    if (nch == 1) {
+        ext[0] = all;
+        per = numPairs;
+    }
+    // device layout: every chunk's windows back to back, 16-byte aligned
+    long long roff[kChunks], qoff[kChunks], rtot = 0, qtot = 0;
+    for (int c = 0; c < nch; c++) {
+        roff[c] = rtot;
+        qoff[c] = qtot;
+        rtot += ((ext[c].rhi - ext[c].rlo) + 15) & ~15LL;
+        qtot += ((ext[c].qhi - ext[c].qlo) + 15) & ~15LL;
+    }
     const size_t pbytes = (size_t)numPairs * sizeof(tal_seq_pair);
     if ((e = h->pairs.ensure(pbytes)) != cudaSuccess ||
-        (e = h->ref.ensure((size_t)(rhi - rlo) + 16)) != cudaSuccess ||
-        (e = h->qer.ensure((size_t)(qhi - qlo) + 16)) != cudaSuccess)
+        (e = h->ref.ensure((size_t)rtot + 16)) != cudaSuccess ||
+        (e = h->qer.ensure((size_t)qtot + 16)) != cudaSuccess)
         return fail(h, TAL_ENOMEM, std::string("device buffers: ") + cudaGetErrorString(e));
-    e = cudaMemcpyAsync(h->pairs.p, pairs, pbytes, cudaMemcpyHostToDevice, h->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(h->ref.p, seqBufRef + rlo, (size_t)(rhi - rlo),
-                            cudaMemcpyHostToDevice, h->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(h->qer.p, seqBufQer + qlo, (size_t)(qhi - qlo),
-                            cudaMemcpyHostToDevice, h->stream);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(H2D)");
-    talbsw::LaunchArgs A;
-    memset(&A, 0, sizeof(A));
-    A.pairs = reinterpret_cast<talbsw::DevPair *>(h->pairs.p);
-    A.ref = reinterpret_cast<const uint8_t *>(h->ref.p);
-    A.qer = reinterpret_cast<const uint8_t *>(h->qer.p);
-    A.ref_lo = rlo; A.ref_hi = rhi; A.qer_lo = qlo; A.qer_hi = qhi;
-    A.order = nullptr;
-    A.wpair = nullptr;
-    A.n = numPairs;
-    A.w = w;
-    A.bits = bits;
-    A.cols_cap = std::max(max2, 1);
-    A.rows_cap = std::max(max1, 1);
-    int rc = launch_scoring(h, A, w);
-    if (rc != TAL_OK) {
-        cudaStreamSynchronize(h->stream);
-        return rc;
+    if (nch > 1 && !h->cstream) {
+        e = cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking);
+        for (int c = 0; c < kChunks && e == cudaSuccess; c++)
+            e = cudaEventCreateWithFlags(&h->cev[c], cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(h, e, "copy stream");
     }
-    rc = collect(h);
+    // the copy stream starts after the previous call's work on the scoring stream
+    if (nch > 1) {
+        if ((e = cudaEventRecord(h->cev[0], h->stream)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(h->cstream, h->cev[0], 0)) != cudaSuccess)
+            return cuda_fail(h, e, "stream order");
+    }
+    for (int c = 0; c < nch; c++) {
+        const int32_t k0 = c * per, k1 = std::min<int32_t>(numPairs, (c + 1) * per);
+        if (k1 <= k0) {
+            nch = c;
+            break;
+        }
+        cudaStream_t cs = nch > 1 ? h->cstream : h->stream;
+        uint8_t *dp = reinterpret_cast<uint8_t *>(h->pairs.p) + (size_t)k0 * sizeof(tal_seq_pair);
+        uint8_t *dr = reinterpret_cast<uint8_t *>(h->ref.p) + roff[c];
+        uint8_t *dq = reinterpret_cast<uint8_t *>(h->qer.p) + qoff[c];
+        e = cudaMemcpyAsync(dp, pairs + k0, (size_t)(k1 - k0) * sizeof(tal_seq_pair),
+                            cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dr, seqBufRef + ext[c].rlo, (size_t)(ext[c].rhi - ext[c].rlo),
+                                cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dq, seqBufQer + ext[c].qlo, (size_t)(ext[c].qhi - ext[c].qlo),
+                                cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess && nch > 1) {
+            e = cudaEventRecord(h->cev[c], cs);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, h->cev[c], 0);
+        }
+        if (e != cudaSuccess) {
+            cudaStreamSynchronize(h->stream);
+            if (h->cstream) cudaStreamSynchronize(h->cstream);
+            return cuda_fail(h, e, "cudaMemcpyAsync(H2D)");
+        }
+        talbsw::LaunchArgs A;
+        memset(&A, 0, sizeof(A));
+        A.pairs = reinterpret_cast<talbsw::DevPair *>(dp);
+        A.ref = dr;
+        A.qer = dq;
+        A.ref_lo = ext[c].rlo; A.ref_hi = ext[c].rhi; A.qer_lo = ext[c].qlo; A.qer_hi = ext[c].qhi;
+        A.order = nullptr;
+        A.wpair = nullptr;
+        A.n = k1 - k0;
+        A.w = w;
+        A.bits = bits;
+        // one row capacity for all chunks: the kernel configuration stays the same
+        A.cols_cap = std::max(all.max2, 1);
+        A.rows_cap = std::max(all.max1, 1);
+        int rc = launch_scoring(h, A, w, c);
+        if (rc != TAL_OK) {
+            cudaStreamSynchronize(h->stream);
+            if (h->cstream) cudaStreamSynchronize(h->cstream);
+            return rc;
+        }
+    }
+    // a bad pair index is local to its chunk: chunks are launched in order, so
+    // map it back through the chunk bounds after the merge
+    int rc = collect_chunks(h, nch, per);
     if (rc != TAL_OK) return rc;
     e = cudaMemcpyAsync(pairs, h->pairs.p, pbytes, cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);

@@ -199,6 +199,9 @@ struct tal_bsw_ctx {
     cudaStream_t stream = nullptr;
     talbsw::DevBuf pairs, ref, qer, ctrl, wpair, caps;
     talbsw::DevBuf porder;  // plain launch: work order by target length, and its buckets
+    // host-buffer calls in chunks: copies on cstream, chunk k's scoring waits on cev[k]
+    cudaStream_t cstream = nullptr;
+    cudaEvent_t cev[4] = {};
     // batched form
     talbsw::DevBuf bcounts, border, bseg, bctrl, btune_seg;
     talbsw::BinFork bfork;
