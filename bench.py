@@ -62,6 +62,9 @@ def parse_args():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
     ap.add_argument("--no-full-sw", action="store_true", help="skip the unbanded Smith-Waterman section")
     ap.add_argument("--no-chain", action="store_true", help="skip the anchor chaining section")
+    ap.add_argument("--no-extend", action="store_true", help="skip the seed-extension section")
+    ap.add_argument("--extend-reads", type=int, default=40_000,
+                    help="reads (100-250 bp, 1-3 seeds each) in the seed-extension section")
     ap.add_argument("--chain-reads", type=int, default=10_000,
                     help="reads (1-10 kb, minimap2-like anchors) in the chaining section")
     ap.add_argument("--sw-pairs", type=int, default=100_000,
@@ -433,6 +436,9 @@ def run_ours(args):
     if not args.no_chain:
         log("anchor chaining")
         result["chain"] = run_chain(args, dist)
+    if not args.no_extend:
+        log("seed extension")
+        result["extend"] = run_extend(args, dist)
     if not args.no_serving:
         log("serving loop")
         peak = result.get("mixed", {}).get("batched", {}).get("pairs_per_s")
@@ -806,6 +812,44 @@ def run_chain(args, dist):
         out["cpu_baseline"] = {"evals_per_s": round(sample_evals / dt, 1), "cores": nth, "kind": "port",
                                "sample": f"first {k} reads ({sub_a.shape[0]} anchors), oracle restatement"}
         out["outputs_match_oracle_sample"] = bool((sf == ef).all() and (sp == ep).all() and (sv == ev).all())
+    return out
+
+
+def run_extend(args, dist):
+    """Caller-side seed extension (include/tal_extend.h) end to end on host
+    buffers: seeds per second, and the cells of its two BSW batches."""
+    import tal_bsw
+    from tal_bsw import seeddata, synth
+    from tal_bsw.extend import extend_seeds
+    b = seeddata.generate(args.extend_reads, seed=55 + dist.rank)
+    P = synth.C2.params()
+    out = {"workload": f"{b.n_reads} reads of U[100,250] bp from a 2 Mb random reference (3% "
+                       f"substitutions, 1-3 bp indels, 10% with a random tail), {b.seeds.shape[0]} "
+                       "exact-match seeds, w = 100, clipping penalties 5 / 5, C2 scoring"}
+    with tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                  P["end_bonus"], None, P["a"], P["b"], 1, device=dist.local) as bsw:
+        for _ in range(2):
+            extend_seeds(bsw, b.ref, b.reads, b.read_off, b.seeds, 100, 5, 5)
+        steps = 3
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            got = extend_seeds(bsw, b.ref, b.reads, b.read_off, b.seeds, 100, 5, 5)
+        t = dist.max((time.perf_counter() - t0) / steps)
+    out["e2e"] = {"seeds_per_s": round(dist.sum(b.seeds.shape[0]) / t, 1), "ms_per_step": round(t * 1e3, 3),
+                  "h2d_bytes_per_step": int(b.ref.nbytes + b.reads.nbytes + b.seeds.nbytes),
+                  "d2h_bytes_per_step": int(got.nbytes)}
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        import oracle
+        k = min(b.seeds.shape[0], 1500)
+        t0 = time.perf_counter()
+        exp = oracle.extend(b.ref, b.reads, b.read_off, b.seeds[:k], P, 100, 5, 5)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"seeds_per_s": round(k / dt, 1), "cores": 1, "kind": "port",
+                               "sample": f"first {k} seeds, oracle restatement (python windows, "
+                                         "C BSW oracle)"}
+        out["outputs_match_oracle_sample"] = bool(all((got[f][:k] == exp[f]).all()
+                                                      for f in ("rb", "re", "qb", "qe", "score")))
     return out
 
 

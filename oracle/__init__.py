@@ -285,3 +285,104 @@ def chain_reference(anchors: np.ndarray, offsets: np.ndarray, params, dr: int, d
     if rc != 0:
         raise RuntimeError("ref_chain_run failed")
     return f, p, v
+
+
+# ---------------------------------------------------------------- seed extension
+def _max_gap(params, n, w):
+    """clamp(max((n*a - o_del) // e_del + 1, (n*a - o_ins) // e_ins + 1), 1, 2w),
+    C integer division (truncation)."""
+    def cdiv(x, y):
+        q = abs(x) // y
+        return q if x >= 0 else -q
+    a = params["a"]
+    d = cdiv(n * a - params["o_del"], params["e_del"]) + 1
+    i = cdiv(n * a - params["o_ins"], params["e_ins"]) + 1
+    return min(max(d, i, 1), 2 * w)
+
+
+def extend(ref: np.ndarray, reads: np.ndarray, read_off: np.ndarray, seeds: np.ndarray,
+           params: Dict[str, int], w: int, pen_clip5: int, pen_clip3: int) -> np.ndarray:
+    """The caller-side seed extension of include/tal_extend.h restated: left
+    pairs (reversed sequences before the seed, h0 = len * a), their clipping
+    choice, right pairs (after the seed, h0 = the left result), the region.
+    Parity unpinned: this stage (BWA-MEM2's mem_chain2aln) is not in the
+    reference; the specification is the header's, the pairs are scored by
+    the pinned BSW oracle (`routed`)."""
+    from tal_bsw.seqpair import SEQPAIR_DTYPE
+    from tal_bsw.seeddata import REGION_DTYPE
+    a = params["a"]
+    n = seeds.shape[0]
+    tparts, qparts, lp, rp = [], [], [], []
+    tpos = qpos = 0
+    left_of = np.full(n, -1, np.int64)
+    right_of = np.full(n, -1, np.int64)
+    for s in range(n):
+        r, qb, rb, ln = int(seeds["read"][s]), int(seeds["qbeg"][s]), int(seeds["rbeg"][s]), int(seeds["len"][s])
+        r0 = int(read_off[r])
+        L = int(read_off[r + 1]) - r0
+        if qb > 0:
+            rs = max(0, rb - qb - _max_gap(params, qb, w))
+            t = ref[rs:rb][::-1]
+            q = reads[r0:r0 + qb][::-1]
+            left_of[s] = len(lp)
+            lp.append((tpos, qpos, s, t.shape[0], q.shape[0], ln * a))
+            tparts.append(t); qparts.append(q)
+            tpos += t.shape[0]; qpos += q.shape[0]
+        qe0, re0 = qb + ln, rb + ln
+        if qe0 < L:
+            ql = L - qe0
+            re = min(ref.shape[0], re0 + ql + _max_gap(params, ql, w))
+            t = ref[re0:re]
+            q = reads[r0 + qe0:r0 + L]
+            right_of[s] = len(rp)
+            rp.append((tpos, qpos, s, t.shape[0], q.shape[0], 0))
+            tparts.append(t); qparts.append(q)
+            tpos += t.shape[0]; qpos += q.shape[0]
+    T = np.concatenate(tparts + [np.zeros(16, np.uint8)]).astype(np.uint8)
+    Q = np.concatenate(qparts + [np.zeros(16, np.uint8)]).astype(np.uint8)
+
+    def mk(rows):
+        p = np.zeros(len(rows), SEQPAIR_DTYPE)
+        for k, (idr, idq, sid, l1, l2, h0) in enumerate(rows):
+            p[k]["idr"], p[k]["idq"], p[k]["id"] = idr, idq, sid
+            p[k]["len1"], p[k]["len2"], p[k]["h0"] = l1, l2, h0
+        for f in ("score", "tle", "gtle", "qle", "gscore", "max_off"):
+            p[f] = -1
+        return p
+
+    L_ = routed(mk(lp), T, Q, w, params, bits=0) if lp else mk([])
+
+    def left_outcome(s):
+        qb, rb, ln = int(seeds["qbeg"][s]), int(seeds["rbeg"][s]), int(seeds["len"][s])
+        k = left_of[s]
+        if k < 0:
+            return qb, rb, ln * a
+        p = L_[k]
+        if p["gscore"] <= 0 or p["gscore"] <= p["score"] - pen_clip5:
+            return qb - int(p["qle"]), rb - int(p["tle"]), int(p["score"])
+        return 0, rb - int(p["gtle"]), int(p["gscore"])
+
+    R = mk(rp)
+    for s in range(n):
+        if right_of[s] >= 0:
+            R[right_of[s]]["h0"] = left_outcome(s)[2]
+    R_ = routed(R, T, Q, w, params, bits=0) if rp else R
+    out = np.zeros(n, REGION_DTYPE)
+    for s in range(n):
+        qb, rb, sc = left_outcome(s)
+        out[s]["qb"], out[s]["rb"], out[s]["left_score"] = qb, rb, sc
+        r = int(seeds["read"][s])
+        L = int(read_off[r + 1] - read_off[r])
+        qe0 = int(seeds["qbeg"][s] + seeds["len"][s])
+        re0 = int(seeds["rbeg"][s] + seeds["len"][s])
+        k = right_of[s]
+        if k < 0:
+            out[s]["qe"], out[s]["re"] = qe0, re0
+        else:
+            p = R_[k]
+            if p["gscore"] <= 0 or p["gscore"] <= p["score"] - pen_clip3:
+                out[s]["qe"], out[s]["re"], sc = qe0 + int(p["qle"]), re0 + int(p["tle"]), int(p["score"])
+            else:
+                out[s]["qe"], out[s]["re"], sc = L, re0 + int(p["gtle"]), int(p["gscore"])
+        out[s]["score"] = sc
+    return out

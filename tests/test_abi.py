@@ -83,12 +83,25 @@ def test_ctypes_structs_match_the_header(tmp_path):
     assert ctypes.sizeof(_Anchor) == ANCHOR_DTYPE.itemsize
     assert [ANCHOR_DTYPE.fields[n][1] for n in ANCHOR_DTYPE.names] == \
         [getattr(_Anchor, n).offset for n, _ in _Anchor._fields_]
+    from tal_bsw.extend import _ExtParams
+    from tal_bsw.seeddata import REGION_DTYPE, SEED_DTYPE
+
+    def _mirror(dt):
+        m = {"<i4": ctypes.c_int32, "<i8": ctypes.c_int64}
+
+        class _S(ctypes.Structure):
+            _fields_ = [(n, m[dt.fields[n][0].str]) for n in dt.names]
+        assert ctypes.sizeof(_S) == dt.itemsize
+        assert [dt.fields[n][1] for n in dt.names] == [getattr(_S, n).offset for n in dt.names]
+        return _S
     structs = {"tal_bsw_server_config": ServerConfig, "tal_bsw_request_info": RequestInfo,
                "tal_bsw_server_stats": ServerStats, "tal_bsw_params": _Params,
                "tal_sw_params": _SwParams, "tal_sw_pair": _SwPair,
-               "tal_chain_params": _ChainParams, "tal_anchor": _Anchor}
+               "tal_chain_params": _ChainParams, "tal_anchor": _Anchor,
+               "tal_extend_params": _ExtParams, "tal_seed": _mirror(SEED_DTYPE),
+               "tal_region": _mirror(REGION_DTYPE)}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "tal_bsw.h"', '#include "tal_sw.h"',
-             '#include "tal_chain.h"', "int main(void) {"]
+             '#include "tal_chain.h"', '#include "tal_extend.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
         for f, _ in py._fields_:

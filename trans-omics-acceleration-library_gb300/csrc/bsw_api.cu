@@ -207,6 +207,9 @@ int tal_bsw_destroy(tal_bsw_handle h) {
         h->bcounts.release();
         h->border.release();
         h->porder.release();
+        for (DevBuf *b : {&h->xref, &h->xreads, &h->xjobs, &h->xpairs, &h->xtarena, &h->xqarena,
+                          &h->xout})
+            b->release();
         h->bseg.release();
         h->bctrl.release();
         h->btune_seg.release();

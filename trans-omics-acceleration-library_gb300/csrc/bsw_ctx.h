@@ -199,6 +199,8 @@ struct tal_bsw_ctx {
     cudaStream_t stream = nullptr;
     talbsw::DevBuf pairs, ref, qer, ctrl, wpair, caps;
     talbsw::DevBuf porder;  // plain launch: work order by target length, and its buckets
+    // seed extension: reference, reads, copy jobs + seeds, pairs, arenas, regions
+    talbsw::DevBuf xref, xreads, xjobs, xpairs, xtarena, xqarena, xout;
     // host-buffer calls in chunks: copies on cstream, chunk k's scoring waits on cev[k]
     cudaStream_t cstream = nullptr;
     cudaEvent_t cev[4] = {};
