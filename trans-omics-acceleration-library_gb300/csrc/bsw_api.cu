@@ -64,9 +64,22 @@ __global__ void plain_count(const talbsw::DevPair *pairs, int n, int *hist) {
         if (sh[t]) atomicAdd(&hist[t], sh[t]);
 }
 
+// Each block places a contiguous chunk of pairs: it counts the chunk per
+// bucket, reserves the chunk's range of every bucket with one global atomic,
+// then hands out positions inside those ranges with shared-memory atomics.
 __global__ void plain_scatter(const talbsw::DevPair *pairs, int n, int *offs, int32_t *order) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        order[atomicAdd(&offs[plain_bucket(pairs[i])], 1)] = i;
+    __shared__ int sh[talbsw::kScanBuckets];
+    const int chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+    for (int t = threadIdx.x; t < talbsw::kScanBuckets; t += blockDim.x) sh[t] = 0;
+    __syncthreads();
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) atomicAdd(&sh[plain_bucket(pairs[i])], 1);
+    __syncthreads();
+    for (int t = threadIdx.x; t < talbsw::kScanBuckets; t += blockDim.x)
+        if (sh[t]) sh[t] = atomicAdd(&offs[t], sh[t]);
+    __syncthreads();
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x)
+        order[atomicAdd(&sh[plain_bucket(pairs[i])], 1)] = i;
 }
 
 cudaError_t enqueue_plain_order(tal_bsw_ctx *h, talbsw::LaunchArgs &A) {
