@@ -73,6 +73,11 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=300, help="requests per load point")
     ap.add_argument("--serve-plain-loads", type=float, nargs="+", default=[0.1, 0.7])
     ap.add_argument("--serve-plain-requests", type=int, default=120)
+    ap.add_argument("--serve-latency-pairs", type=int, default=0,
+                    help="ticks below this many pairs use the latency launches (0: library default)")
+    ap.add_argument("--serve-slots", type=int, default=0, help="ticks in flight (0: library default)")
+    ap.add_argument("--serve-peak", type=float, default=0.0,
+                    help="pairs/s the load fractions refer to (0: the measured batched peak)")
     ap.add_argument("--serve-pool-pairs", type=int, default=3_000_000,
                     help="pairs the serving requests are drawn from")
     return ap.parse_args()
@@ -442,6 +447,8 @@ def run_ours(args):
     if not args.no_serving:
         log("serving loop")
         peak = result.get("mixed", {}).get("batched", {}).get("pairs_per_s")
+        if args.serve_peak > 0:
+            peak = args.serve_peak * dist.ws
         result["serving"] = run_serving(args, dist, peak / dist.ws if peak else None)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         log("cpu baseline")
@@ -592,7 +599,8 @@ def run_serving(args, dist, peak_pairs_per_s):
     out = {"workload": f"requests of log-uniform size in [{lo_n}, {hi_n}] pairs (mean {mean_req:.0f}) "
                        f"drawn from c3_mixed ({npool} pooled pairs), Poisson arrivals",
            "batched_peak_pairs_per_s": round(peak_pairs_per_s, 1), "points": []}
-    srv = BswServer(bsw)                       # pool: min(64 GiB, 85 % of free HBM)
+    # pool: min(64 GiB, 85 % of free HBM)
+    srv = BswServer(bsw, slots=args.serve_slots, latency_pairs=args.serve_latency_pairs)
     infos = {}
 
     def s_submit(lo, n):

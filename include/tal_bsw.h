@@ -214,7 +214,7 @@ typedef struct {
     size_t staging_bytes;   /* pinned host staging for pageable callers; 0 = 1 GiB */
     int32_t max_tick_pairs; /* most pairs in one tick (and in one request);
                                0 = 8,388,608 */
-    int32_t slots;          /* ticks on the device at once, 1..4; 0 = 4 */
+    int32_t slots;          /* ticks on the device at once, 1..4; 0 = 2 */
     int32_t latency_pairs;  /* ticks with fewer pairs run as a handful of
                                launches with several lanes per pair above 256
                                columns (lower latency per pair); larger ticks
