@@ -59,7 +59,9 @@ static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
                 simt::tl_smem = a.sm;
                 if (a.ch) { talchain::chain_kernel(*a.ch); a.W->done[a.t & 31] = true; return; }
                 if (a.sw) { if (sw_packed) talsw::sw_wave2_kernel<talsw::kSwRows>(*a.sw); else talsw::sw_wave_kernel<talsw::kSwRows>(*a.sw); a.W->done[a.t & 31] = true; return; }
-                if (a.G == 1) { const bool sym = a.A->P.o_del == a.A->P.o_ins && a.A->P.e_del == a.A->P.e_ins; int v = a.K == 4 ? 3 : a.K == 2 ? 2 : 1; if (!sym) v &= 1; if (v == 3) talbsw::bsw_lane_kernel<3>(*a.A); else if (v == 2) talbsw::bsw_lane_kernel<2>(*a.A); else if (v == 1) talbsw::bsw_lane_kernel<1>(*a.A); else talbsw::bsw_lane_kernel<0>(*a.A); a.W->done[a.t & 31] = true; return; }
+                if (a.G == 1) { const bool sym = a.A->P.o_del == a.A->P.o_ins && a.A->P.e_del == a.A->P.e_ins; int v = a.K == 4 ? 3 : a.K == 2 ? 2 : 1; if (!sym) v &= 1; if (a.A->win > 0 && (a.A->win & (a.A->win - 1))) v |= 4;
+                    switch (v) { case 7: talbsw::bsw_lane_kernel<7>(*a.A); break; case 6: talbsw::bsw_lane_kernel<6>(*a.A); break; case 5: talbsw::bsw_lane_kernel<5>(*a.A); break; case 4: talbsw::bsw_lane_kernel<4>(*a.A); break; case 3: talbsw::bsw_lane_kernel<3>(*a.A); break; case 2: talbsw::bsw_lane_kernel<2>(*a.A); break; case 1: talbsw::bsw_lane_kernel<1>(*a.A); break; default: talbsw::bsw_lane_kernel<0>(*a.A); }
+                    a.W->done[a.t & 31] = true; return; }
                 switch (a.G * 10 + a.K) {
                     case 44: talbsw::bsw_kernel<4, 4>(*a.A); break;
                     case 42: talbsw::bsw_kernel<4, 2>(*a.A); break;

@@ -127,6 +127,7 @@ inline void __syncwarp(unsigned = 0xffffffffu) { simt::tl_warp->barrier(simt::la
 // Block barriers appear only in kernels the emulator never runs (the work
 // order sort); warps here run one after another, so none could be honoured.
 inline void __syncthreads() { std::abort(); }
+inline unsigned __umulhi(unsigned a, unsigned b) { return (unsigned)(((unsigned long long)a * b) >> 32); }
 inline int __ffs(unsigned x) { return x ? __builtin_ctz(x) + 1 : 0; }
 inline int __clz(unsigned x) { return x ? __builtin_clz(x) : 32; }
 inline int __popc(unsigned x) { return __builtin_popcount(x); }

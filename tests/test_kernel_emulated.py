@@ -298,3 +298,20 @@ def test_emulated_chain_kernel_windows_past_the_ring():
     assert flags == 0 and n0 > 2000
     assert evals > 1100 * n0  # windows wider than the ring
     assert (gf == ef).all() and (gp == ep).all() and (gv == ev).all()
+
+
+@pytest.mark.parametrize("win", [224, 96, 320])
+def test_emulated_lane_kernel_exact_rings(win):
+    """Lane-kernel rings of any multiple of 32 columns (column j in slot j mod
+    W by a multiply-high; the group loop's slot advances by four and wraps),
+    e.g. the plain launch's 224 columns for band 100, against the oracle."""
+    from tal_bsw import synth
+    b = synth.generate(synth.C2, 48)
+    P = synth.C2.params()
+    w = (win - 12) // 2
+    exp = oracle.vector(b.pairs, b.ref, b.qer, w, P, bits=16, lanes=1)
+    got, ef, _ = simt_emu.run(b.pairs, b.ref, b.qer, w, P, bits=16, K=4, G=1, warps=1, win=win)
+    assert ef == 0
+    e, g = outputs(exp), outputs(got)
+    bad = np.nonzero((e != g).any(1))[0]
+    assert bad.size == 0, f"win={win}: pair {bad[0]}: emu {g[bad[0]].tolist()} oracle {e[bad[0]].tolist()}"

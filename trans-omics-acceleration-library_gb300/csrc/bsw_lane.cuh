@@ -60,6 +60,13 @@ __host__ __device__ __forceinline__ int lane_window_for(long long w) {
     return lane_ring_at_least(2 * w + 12);
 }
 
+// The lane kernel's ring for band w: 2w + 12 columns rounded up to a
+// multiple of 32 (the lane kernel maps columns to slots by a remainder; the
+// G kernel's rings are powers of two).
+__host__ __device__ __forceinline__ int lane_ring_exact(long long w) {
+    return (int)((2 * w + 12 + 31) & ~31LL);
+}
+
 // Score of query code q (0..4) against the row's table, sign-extended.
 __device__ __forceinline__ int lane_score1(uint32_t tlo, uint32_t thi, uint32_t q) {
     return prmt_sext(__byte_perm(tlo, thi, q), 0u, 0x8880u);
@@ -139,10 +146,13 @@ struct LanePair {
 };
 
 // V bit 0: plain group loop (else explicit prefetch of the next group);
-// V bit 1: symmetric gap parameters (o_del == o_ins, e_del == e_ins).
+// V bit 1: symmetric gap parameters (o_del == o_ins, e_del == e_ins);
+// V bit 2: a ring of any multiple of 8 columns (else a power of two, or
+// whole rows).
 template <int V>
 __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
     constexpr bool SYM = (V & 2) != 0;
+    constexpr bool EXACT = (V & 4) != 0;
     TALBSW_DYNAMIC_SMEM(smem_raw);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -150,10 +160,19 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                     (size_t)wib * (lane_hf_words(A.cols_cap, A.win) + lane_qs_words(A.cols_cap, A.win));
     uint32_t *HF = wsm + lane;                                     // column j: HF[slot(j) * 32]
     uint32_t *QS = wsm + lane_hf_words(A.cols_cap, A.win) + lane;  // columns 8q..8q+7: QS[qslot(q) * 32]
-    const int wm = A.win > 0 ? A.win - 1 : -1;  // column -> slot mask (-1: whole rows)
-    const int qm = wm >> 3;                     // query word -> slot mask
-    auto hf = [&](int j) -> uint32_t & { return HF[(uint32_t)(j & wm) << 5]; };
-    auto qs = [&](int j) -> uint32_t & { return QS[(uint32_t)((j >> 3) & qm) << 5]; };
+    // column j -> ring slot: j mod W (a multiply-high by ceil(2^32 / W),
+    // exact for j < 2^16, in a ring of any multiple of 8 columns; a mask in a
+    // power-of-two ring; j itself in whole rows).  Query word of column j:
+    // slot >> 3 (W is a multiple of 8).
+    const uint32_t W = A.win > 0 ? (uint32_t)A.win : 0u;
+    const uint32_t wmask = W ? W - 1 : 0xffffffffu;
+    const uint32_t mg = EXACT ? (uint32_t)((0x100000000ULL + W - 1) / W) : 0u;
+    auto slot = [&](uint32_t j) -> uint32_t {
+        if constexpr (EXACT) return j - W * __umulhi(j, mg);
+        else return j & wmask;
+    };
+    auto hf = [&](int j) -> uint32_t & { return HF[slot((uint32_t)j) << 5]; };
+    auto qs = [&](int j) -> uint32_t & { return QS[(slot((uint32_t)j) >> 3) << 5]; };
     const KernelParams P = A.P;
     const int oe_ins = P.o_ins + P.e_ins, oe_del = P.o_del + P.e_del;
     const int e_ins = P.e_ins, e_del = P.e_del;
@@ -382,12 +401,18 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             } else {
                 // plain loop over groups; two groups per iteration so that
                 // the second group's loads can be issued early
+                // the group's slot advances by four (j is a multiple of 4, and
+                // so is W: a group never straddles the ring's end)
+                uint32_t sj = j + 3 < jB ? slot((uint32_t)j) : 0u;
 #pragma unroll 2
                 for (; j + 3 < jB; j += 4) {
-                    uint32_t *hp = &hf(j);
-                    const uint32_t qw = qs(j) >> (4 * (j & 4));
+                    uint32_t *hp = &HF[sj << 5];
+                    const uint32_t qw = QS[(sj >> 3) << 5] >> (4 * (j & 4));
                     lane_group4<SYM>(hp, j, hp[0], hp[32], hp[64], hp[96], qw, tlo, thi, e, hprev,
                                      key, oe_ins, e_ins, oe_del, e_del);
+                    sj += 4;
+                    if constexpr (EXACT) sj = sj >= W ? sj - W : sj;
+                    else sj &= wmask;
                 }
             }
             for (; j < jB; j++) {
@@ -475,7 +500,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                 // scan stops inside the band
                 int l = E;
                 while (l >= B && hf(l) == 0u) l--;
-                if (l < beg && wm >= 0) {  // would have read a ring slot reused since
+                if (l < beg && W > 0) {  // would have read a ring slot reused since
                     fail(ERR_CAPACITY, s.req, s.pidx);
                     active = false;
                     continue;

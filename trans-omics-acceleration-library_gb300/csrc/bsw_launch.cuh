@@ -30,7 +30,10 @@ constexpr int kLaneMaxCols = 384;
 // <= cols_cap: 0 (whole rows) unless a ring is smaller.
 inline int lane_window(long long w, int cols_cap) {
     if (w < 0) return 0;
-    const int W = lane_window_for(w);
+    // sized exactly (a multiple of 32) when the lane kernel takes it, a power
+    // of two when the G kernel does (TAL_BSW_POW2_RING: always, for tuning)
+    int W = lane_ring_exact(w);
+    if (W - 4 > kLaneMaxCols || getenv("TAL_BSW_POW2_RING")) W = lane_window_for(w);
     return W < cols_cap + 4 ? W : 0;
 }
 
@@ -108,8 +111,18 @@ inline cudaError_t launch_lane(const LaunchArgs &A, int num_sms, size_t smem_opt
     int v = sym ? 3 : 1;
     if (const char *ev = getenv("TAL_BSW_LV")) v = atoi(ev) & 3;
     if (!sym) v &= 1;
-    auto kern = v == 0 ? bsw_lane_kernel<0> : v == 1 ? bsw_lane_kernel<1>
-              : v == 2 ? bsw_lane_kernel<2> : bsw_lane_kernel<3>;
+    if (A.win > 0 && (A.win & (A.win - 1)) != 0) v |= 4;  // a ring that is not a power of two
+    void (*kern)(LaunchArgs);
+    switch (v) {
+        case 0: kern = bsw_lane_kernel<0>; break;
+        case 1: kern = bsw_lane_kernel<1>; break;
+        case 2: kern = bsw_lane_kernel<2>; break;
+        case 3: kern = bsw_lane_kernel<3>; break;
+        case 4: kern = bsw_lane_kernel<4>; break;
+        case 5: kern = bsw_lane_kernel<5>; break;
+        case 6: kern = bsw_lane_kernel<6>; break;
+        default: kern = bsw_lane_kernel<7>; break;
+    }
     const size_t wbytes = lane_warp_smem_bytes(A.cols_cap, A.win);
     int wpb = 4;
     while (wpb > 1 && (size_t)wpb * wbytes > 48 * 1024) wpb >>= 1;
