@@ -791,11 +791,14 @@ def run_chain(args, dist):
         ha = torch.empty(b.anchors.nbytes, dtype=torch.uint8, pin_memory=True)
         ha.numpy()[:] = b.anchors.view(np.uint8)
         anchors_pinned = ha.numpy().view(chaindata.ANCHOR_DTYPE)
-        ch.mm_dp_batch(anchors_pinned, b.offsets, dr, dq)
+        outs_t = [torch.empty(4 * n, dtype=torch.uint8, pin_memory=True) for _ in range(3)]
+        outs = (outs_t[0].numpy().view(np.uint32), outs_t[1].numpy().view(np.int32),
+                outs_t[2].numpy().view(np.int32))
+        ch.mm_dp_batch(anchors_pinned, b.offsets, dr, dq, out=outs)
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(steps):
-            gf, gp, gv = ch.mm_dp_batch(anchors_pinned, b.offsets, dr, dq)
+            gf, gp, gv = ch.mm_dp_batch(anchors_pinned, b.offsets, dr, dq, out=outs)
         te = dist.max((time.perf_counter() - t0) / steps)
         out["e2e"] = {"evals_per_s": round(dist.sum(evals) / te, 1),
                       "anchors_per_s": round(dist.sum(n) / te, 1), "ms_per_step": round(te * 1e3, 3),

@@ -75,14 +75,21 @@ class dp_chain:  # noqa: N801 -- the reference's class name
         self._check(self._lib.tal_chain_dp(self._h, anchors.ctypes.data, offs.ctypes.data, 1, int(dr),
                                            int(dq), f.ctypes.data, p.ctypes.data, v.ctypes.data))
 
-    def mm_dp_batch(self, anchors: np.ndarray, offsets: np.ndarray, dr: int, dq: int):
-        """Reads anchors[offsets[k], offsets[k+1]); returns (f, p, v) for all anchors."""
+    def mm_dp_batch(self, anchors: np.ndarray, offsets: np.ndarray, dr: int, dq: int, out=None):
+        """Reads anchors[offsets[k], offsets[k+1]); returns (f, p, v) for all
+        anchors -- written into `out` = (f, p, v) when given (e.g. pinned
+        host arrays, which the device copies into directly)."""
         offsets = np.ascontiguousarray(offsets, np.int64)
         n = int(offsets[-1]) if offsets.shape[0] else 0
         _check_array(anchors, ANCHOR_DTYPE, n, "anchors")
-        f = np.zeros(anchors.shape[0], np.uint32)
-        p = np.zeros(anchors.shape[0], np.int32)
-        v = np.zeros(anchors.shape[0], np.int32)
+        if out is None:
+            f = np.zeros(anchors.shape[0], np.uint32)
+            p = np.zeros(anchors.shape[0], np.int32)
+            v = np.zeros(anchors.shape[0], np.int32)
+        else:
+            f, p, v = out
+            for a, dt, nm in ((f, np.uint32, "f"), (p, np.int32, "p"), (v, np.int32, "v")):
+                _check_array(a, np.dtype(dt), n, nm)
         self._check(self._lib.tal_chain_dp(self._h, anchors.ctypes.data, offsets.ctypes.data,
                                            offsets.shape[0] - 1, int(dr), int(dq), f.ctypes.data,
                                            p.ctypes.data, v.ctypes.data))
