@@ -25,7 +25,9 @@
  *     re = rbeg + len + gtle, sc = gscore.  Without one: qe = qbeg + len,
  *     re = rbeg + len.
  * All left extensions of a call are one batch, all right ones another, both
- * through the plain device launch (8/16-bit routing per pair).
+ * through the plain device launch (8/16-bit routing per pair).  The call uses
+ * the handle's stream and buffers: do not run it concurrently with other
+ * calls on the same handle.
  */
 #ifndef TAL_EXTEND_H
 #define TAL_EXTEND_H
