@@ -153,6 +153,12 @@ int64_t tal_bsw_last_bad_pair(tal_bsw_handle h);
 /* Number of kernel launches this handle has issued (for accounting). */
 uint64_t tal_bsw_launch_count(tal_bsw_handle h);
 
+/* Device time, in milliseconds, of the scoring kernel of the last collected
+ * plain call (tal_bsw_scores / tal_bsw_scores_device + tal_bsw_sync; for a
+ * chunked host call, its last chunk's), from CUDA events on the handle's
+ * stream around that one launch. */
+float tal_bsw_last_kernel_ms(tal_bsw_handle h);
+
 /* DP cells the last collected call computed (sum over rows of the band
  * width the reference's vector kernel visits for each pair).  The reference's
  * own counter, BandedPairWiseSW::SW_cells, is never incremented

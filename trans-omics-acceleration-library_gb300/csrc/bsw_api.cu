@@ -129,7 +129,9 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k, int slot =
     if (A.order == nullptr && A.n >= kOrderMin && !getenv("TAL_BSW_NO_ORDER")) {
         if ((e = enqueue_plain_order(h, A)) != cudaSuccess) return cuda_fail(h, e, "work order");
     }
+    if (h->kev0) cudaEventRecord(h->kev0, h->stream);
     e = talbsw::launch_config(A, cfg, h->num_sms, h->smem_optin, h->stream);
+    if (h->kev1) cudaEventRecord(h->kev1, h->stream);
     h->launches++;
     if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
     return TAL_OK;
@@ -144,6 +146,8 @@ int collect_chunks(tal_bsw_ctx *h, int nslots, int32_t per) {
                                     h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "scoring");
+    if (h->kev0 && h->kev1 && cudaEventElapsedTime(&h->last_kernel_ms, h->kev0, h->kev1) != cudaSuccess)
+        h->last_kernel_ms = 0.f;
     Ctrl c = {0, 0, (long long)INT64_MAX, 0ull};
     for (int k = 0; k < nslots; k++) {
         c.flags |= cs[k].flags;
@@ -195,7 +199,11 @@ int tal_bsw_create(const tal_bsw_params *params, int device, tal_bsw_handle *out
     h->smem_optin = prop.sharedMemPerBlockOptin;
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = h->ctrl.ensure(sizeof(Ctrl) * kChunks);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->kev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->kev1);
     if (e != cudaSuccess) {
+        if (h->kev0) cudaEventDestroy(h->kev0);
+        if (h->kev1) cudaEventDestroy(h->kev1);
         if (h->stream) cudaStreamDestroy(h->stream);
         h->ctrl.release();
         delete h;
@@ -231,6 +239,8 @@ int tal_bsw_destroy(tal_bsw_handle h) {
         h->graphs.clear();
         for (cudaEvent_t &ev : h->cev)
             if (ev) cudaEventDestroy(ev);
+        if (h->kev0) cudaEventDestroy(h->kev0);
+        if (h->kev1) cudaEventDestroy(h->kev1);
         if (h->cstream) cudaStreamDestroy(h->cstream);
         cudaStreamDestroy(h->stream);
     }
@@ -555,6 +565,8 @@ const char *tal_bsw_last_error(tal_bsw_handle h) { return h ? h->last_error.c_st
 int64_t tal_bsw_last_bad_pair(tal_bsw_handle h) { return h ? h->last_bad : -1; }
 
 uint64_t tal_bsw_launch_count(tal_bsw_handle h) { return h ? h->launches : 0; }
+
+float tal_bsw_last_kernel_ms(tal_bsw_handle h) { return h ? h->last_kernel_ms : 0.f; }
 
 uint64_t tal_bsw_last_cells(tal_bsw_handle h) { return h ? h->last_cells : 0; }
 

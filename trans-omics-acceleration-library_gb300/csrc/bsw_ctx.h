@@ -204,6 +204,9 @@ struct tal_bsw_ctx {
     // host-buffer calls in chunks: copies on cstream, chunk k's scoring waits on cev[k]
     cudaStream_t cstream = nullptr;
     cudaEvent_t cev[4] = {};
+    // around the last scoring launch (plain calls): its device time
+    cudaEvent_t kev0 = nullptr, kev1 = nullptr;
+    float last_kernel_ms = 0.f;
     // batched form
     talbsw::DevBuf bcounts, border, bseg, bctrl, btune_seg;
     talbsw::BinFork bfork;

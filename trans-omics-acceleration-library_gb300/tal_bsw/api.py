@@ -52,6 +52,7 @@ _SIGS = {
     "tal_bsw_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "tal_bsw_last_bad_pair": (ctypes.c_int64, [ctypes.c_void_p]),
     "tal_bsw_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "tal_bsw_last_kernel_ms": (ctypes.c_float, [ctypes.c_void_p]),
     "tal_bsw_last_cells": (ctypes.c_uint64, [ctypes.c_void_p]),
     "tal_bsw_scores_batched_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                      ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
@@ -231,6 +232,11 @@ class BandedPairWiseSW:
     @property
     def launch_count(self) -> int:
         return int(self._lib.tal_bsw_launch_count(self._h))
+
+    @property
+    def last_kernel_ms(self) -> float:
+        """Device time of the last plain call's scoring kernel (CUDA events)."""
+        return float(self._lib.tal_bsw_last_kernel_ms(self._h))
 
     @property
     def last_cells(self) -> int:
