@@ -84,7 +84,11 @@ int tal_bsw_destroy(tal_bsw_handle h);
  * h0 + w_match * min(len1, len2) <= 127 (the reference's own 8-bit limits,
  * bandedSWA.h:82 and the int8 score range) plus two no-wrap conditions on
  * the first column and the gap scores.  A pair outside it gives TAL_EDOMAIN
- * (for AUTO: outside both), and no outputs are written. */
+ * (for AUTO: outside both), and no outputs are written.  Capacity: a pair's
+ * rows live in shared memory, as a ring of the band's columns (2w + 12 up to
+ * 16,384, any query length) or as whole rows (queries up to ~22,000 bases);
+ * a pair that fits neither (a query above ~22,000 bases with w above 8,186)
+ * also gives TAL_EDOMAIN. */
 int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufRef,
                    const uint8_t *seqBufQer, int32_t numPairs, int32_t w, int bits);
 

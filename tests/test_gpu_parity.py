@@ -166,3 +166,32 @@ def test_host_call_in_chunks():
             bsw.getScores16(g2, b.ref, q, b.n, 1, 100)
         assert ei.value.bad_pair == bad
         assert (outputs(g2) == -1).all(), "no outputs are written on an error"
+
+
+def test_long_queries_near_the_16_bit_limit():
+    """Queries of 20,000-32,700 bases: narrow bands in rings (lane kernel),
+    a band of 8,000 in a 16,384-column ring (G lanes per pair), a band of
+    10,000 in whole rows of 22,000 columns; a query of 30,000 with a band of
+    20,000 needs more shared memory than a block has: TAL_EDOMAIN."""
+    from _cases import DEFAULT, pack
+    rng = np.random.default_rng(77)
+
+    def pair(L, extra):
+        q = rng.integers(0, 4, L).astype(np.uint8)
+        r = q.copy()
+        m = rng.random(L) < 0.03
+        r[m] = (r[m] + 1) % 4
+        return np.concatenate([r, rng.integers(0, 4, extra).astype(np.uint8)]), q
+
+    for lens, w in (((30000, 32700, 20000), 50), ((20000,), 8000), ((22000,), 10000)):
+        refs, qers = zip(*[pair(L, 40) for L in lens])  # h0 + min length stays below 2^15
+        p, r, q = pack(list(refs), list(qers), [50] * len(lens))
+        exp = oracle.vector(p, r, q, w, DEFAULT, bits=16)
+        got = _gpu(p, r, q, w, DEFAULT, 16)
+        _assert_same(exp, got, f"long queries, w={w}")
+    refs, qers = zip(*[pair(30000, 0)])
+    p, r, q = pack(list(refs), list(qers), [50])
+    with _bsw(DEFAULT) as bsw:
+        with pytest.raises(tal_bsw.TalBswError) as ei:
+            bsw.getScores16(p.copy(), r, q, 1, 1, 20000)
+        assert ei.value.status == tal_bsw.api.TAL_EDOMAIN
