@@ -39,7 +39,22 @@ enum {
 enum {
     TAL_BSW_AUTO = 0, /* per pair: 8-bit rules where eligible, else 16-bit */
     TAL_BSW_8 = 8,    /* getScores8  (bandedSWA.h:257-262) */
-    TAL_BSW_16 = 16   /* getScores16 (bandedSWA.h:285-290) */
+    TAL_BSW_16 = 16,  /* getScores16 (bandedSWA.h:285-290) */
+    /* OR into TAL_BSW_8 / TAL_BSW_16 for tal_bsw_scores and
+     * tal_bsw_scores_device (one band per call, no d_w): score the pairs in
+     * the reference's own SIMD groups -- 64 (8-bit) / 32 (16-bit) consecutive
+     * pairs of the array, the AVX-512BW widths, the last group padded as the
+     * reference pads it -- with the band each group shares, so that every
+     * output equals the reference's on any input.  Without it each pair is
+     * scored as if alone in its group: the same outputs except where a pair's
+     * band is narrow next to its group's (bandedSWA.cpp:3235-3316 re-derive a
+     * lane's head and tail from the group's band edges); that never happened
+     * on the benchmark workloads and happens to about 1 pair in 500 of
+     * seed-extension batches at bands 4-8.  Grouped scoring computes every
+     * value in the reference's wrapping int8 / int16, so its exact range is
+     * only len1, len2 <= 127 (8-bit) / 32767 (16-bit) and h0 >= 0; it runs one
+     * warp per group and is several times slower than the per-pair kernels. */
+    TAL_BSW_GROUPED = 0x100
 };
 
 /* SeqPair, bandedSWA.h:90-99: 14 x int32 = 56 bytes, fields in this order. */

@@ -25,7 +25,10 @@
  *     re = rbeg + len + gtle, sc = gscore.  Without one: qe = qbeg + len,
  *     re = rbeg + len.
  * All left extensions of a call are one batch, all right ones another, both
- * through the plain device launch (8/16-bit routing per pair).  The call uses
+ * through the plain device launch (8/16-bit routing per pair); with band
+ * retries, the pairs that go again form a smaller batch per attempt, on the
+ * same windows (the right batch starts after the left one's last attempt).
+ * The call uses
  * the handle's stream and buffers: do not run it concurrently with other
  * calls on the same handle.
  */
@@ -55,7 +58,12 @@ typedef struct tal_extend_params {
     int32_t w;          /* band of both extensions */
     int32_t pen_clip5;  /* left clipping penalty */
     int32_t pen_clip3;  /* right clipping penalty */
-    int32_t pad_;
+    int32_t band_tries; /* attempts per extension, band w << i (0 or 1: one; BWA-MEM uses 2;
+                           at most 8, and w << (band_tries - 1) at most 2^24):
+                           an extension is run again with the doubled band while its score
+                           changed from the previous attempt's (or it is the first) and its
+                           max_off >= (band >> 1) + (band >> 2); the last attempt's result
+                           stands */
 } tal_extend_params;
 
 /* The region a seed extends to: reference [rb, re), read [qb, qe), its score,

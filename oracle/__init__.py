@@ -155,11 +155,12 @@ def eligible8(pairs: np.ndarray, w, params: Dict[str, int]) -> np.ndarray:
 
 
 def routed(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w, params: Dict[str, int],
-           bits: int = 0, nthreads: int = 1) -> np.ndarray:
+           bits: int = 0, nthreads: int = 1, lanes: Optional[int] = None) -> np.ndarray:
     """Scores every pair with getScores8 or getScores16 semantics: bits 8/16
     forces one; bits 0 routes each pair by eligible8().  w may be a scalar or
-    a per-pair array (pairs are grouped by band; results do not depend on
-    grouping)."""
+    a per-pair array (the pairs of each band and precision, in order, form
+    one call).  lanes: SIMD group width (default: the reference's 32 / 64;
+    1 scores every pair alone, as the library's per-pair kernels do)."""
     out = np.ascontiguousarray(pairs).copy()
     n = out.shape[0]
     if n == 0:
@@ -175,7 +176,8 @@ def routed(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w, params: Dict[
         for b in (8, 16):
             sel = np.nonzero((warr == wv) & (is8 == (b == 8)))[0]
             if sel.size:
-                out[sel] = vector(out[sel], ref, qer, int(wv), params, bits=b, nthreads=nthreads)
+                out[sel] = vector(out[sel], ref, qer, int(wv), params, bits=b, lanes=lanes,
+                                  nthreads=nthreads)
     return out
 
 
@@ -300,14 +302,39 @@ def _max_gap(params, n, w):
     return min(max(d, i, 1), 2 * w)
 
 
+def _scored_with_tries(P: np.ndarray, T: np.ndarray, Q: np.ndarray, w: int, params: Dict[str, int],
+                       tries: int) -> np.ndarray:
+    """Scores the batch P at band w, then, per pair, again at band w << i
+    while its last attempt changed the score (the first always counts) and
+    reached max_off >= (band >> 1) + (band >> 2); the last attempt stands."""
+    R = routed(P, T, Q, w, params, bits=0, lanes=1)
+    prev = np.full(P.shape[0], -1, np.int64)
+    active = np.ones(P.shape[0], bool)
+    for i in range(1, max(1, tries)):
+        wp = w << (i - 1)
+        go = active & (R["score"] != prev) & (R["max_off"] >= (wp >> 1) + (wp >> 2))
+        active = go
+        if not go.any():
+            break
+        prev[go] = R["score"][go]
+        sub = R[go].copy()
+        for f in ("score", "tle", "gtle", "qle", "gscore", "max_off"):
+            sub[f] = -1
+        R[go] = routed(sub, T, Q, w << i, params, bits=0, lanes=1)
+    return R
+
+
 def extend(ref: np.ndarray, reads: np.ndarray, read_off: np.ndarray, seeds: np.ndarray,
-           params: Dict[str, int], w: int, pen_clip5: int, pen_clip3: int) -> np.ndarray:
+           params: Dict[str, int], w: int, pen_clip5: int, pen_clip3: int,
+           band_tries: int = 1) -> np.ndarray:
     """The caller-side seed extension of include/tal_extend.h restated: left
     pairs (reversed sequences before the seed, h0 = len * a), their clipping
-    choice, right pairs (after the seed, h0 = the left result), the region.
+    choice, right pairs (after the seed, h0 = the left result), the region,
+    with BWA-MEM's band-doubling retries when band_tries > 1.
     Parity unpinned: this stage (BWA-MEM2's mem_chain2aln) is not in the
     reference; the specification is the header's, the pairs are scored by
-    the pinned BSW oracle (`routed`)."""
+    the pinned BSW oracle (`routed`), each pair alone in its SIMD group as
+    the library's extension layer scores them."""
     from tal_bsw.seqpair import SEQPAIR_DTYPE
     from tal_bsw.seeddata import REGION_DTYPE
     a = params["a"]
@@ -350,7 +377,7 @@ def extend(ref: np.ndarray, reads: np.ndarray, read_off: np.ndarray, seeds: np.n
             p[f] = -1
         return p
 
-    L_ = routed(mk(lp), T, Q, w, params, bits=0) if lp else mk([])
+    L_ = _scored_with_tries(mk(lp), T, Q, w, params, band_tries) if lp else mk([])
 
     def left_outcome(s):
         qb, rb, ln = int(seeds["qbeg"][s]), int(seeds["rbeg"][s]), int(seeds["len"][s])
@@ -366,7 +393,7 @@ def extend(ref: np.ndarray, reads: np.ndarray, read_off: np.ndarray, seeds: np.n
     for s in range(n):
         if right_of[s] >= 0:
             R[right_of[s]]["h0"] = left_outcome(s)[2]
-    R_ = routed(R, T, Q, w, params, bits=0) if rp else R
+    R_ = _scored_with_tries(R, T, Q, w, params, band_tries) if rp else R
     out = np.zeros(n, REGION_DTYPE)
     for s in range(n):
         qb, rb, sc = left_outcome(s)

@@ -113,3 +113,59 @@ def workload_slices(n_scale=1.0):
         wl = synth.WORKLOADS[name]
         res.append((name, synth.generate(wl, max(1, int(n * n_scale))), wl.bits))
     return res
+
+
+def extension_pairs(n_reads, w, len_lo, len_hi, seed, P=DEFAULT):
+    """The right-extension SeqPair batch of a seed-extension call (targets:
+    the reference after each seed plus the gap allowance, queries: the read
+    after the seed, h0 = the seed length), in seed order: the kind of batch
+    where a narrow band makes a lane's outputs depend on its SIMD group."""
+    from tal_bsw import seeddata
+    b = seeddata.generate(n_reads, len_lo=len_lo, len_hi=len_hi, junk=0.2, indel=0.02, seed=seed)
+
+    def gap(n):
+        d = (n * P["a"] - P["o_del"]) // P["e_del"] + 1
+        i = (n * P["a"] - P["o_ins"]) // P["e_ins"] + 1
+        return min(max(d, i, 1), 2 * w)
+
+    ts, qs, h0s = [], [], []
+    for sd in b.seeds:
+        r = int(sd["read"])
+        r0, L = int(b.read_off[r]), int(b.read_off[r + 1] - b.read_off[r])
+        qe0, re0 = int(sd["qbeg"] + sd["len"]), int(sd["rbeg"] + sd["len"])
+        if qe0 >= L:
+            continue
+        ql = L - qe0
+        ts.append(b.ref[re0:min(b.ref.shape[0], re0 + ql + gap(ql))])
+        qs.append(b.reads[r0 + qe0:r0 + L])
+        h0s.append(int(sd["len"]) * P["a"])
+    return pack(ts, qs, h0s)
+
+
+def coupled_cases():
+    """Pair sets, in SIMD-group order, whose reference outputs depend on the
+    grouping: for each configuration, the 32- (16-bit) or 64-pair (8-bit)
+    groups of an extension batch that hold a pair whose grouped outputs
+    differ from its outputs alone, plus the two groups after each.  Yields
+    (name, pairs, ref, qer, w, bits); the grouping to keep is consecutive
+    groups from the first pair."""
+    import oracle
+    from tal_bsw.seqpair import outputs
+    for name, bits, w, lo, hi, seed in (("coupled16_band_4", 16, 4, 60, 300, 6),
+                                        ("coupled16_band_8", 16, 8, 60, 300, 1),
+                                        ("coupled8_band_8", 8, 8, 40, 127, 8)):
+        p, ref, qer = extension_pairs(1500, w, lo, hi, seed)
+        if bits == 8:
+            keep = (p["len1"] <= 127) & (p["len2"] <= 127) & (p["h0"] + np.minimum(p["len1"], p["len2"]) <= 127)
+            p = p[keep]
+        lanes = 64 if bits == 8 else 32
+        grp = oracle.vector(p, ref, qer, w, DEFAULT, bits=bits)
+        one = oracle.vector(p, ref, qer, w, DEFAULT, bits=bits, lanes=1)
+        hit = np.nonzero((outputs(grp) != outputs(one)).any(1))[0] // lanes
+        gs = sorted({int(g + d) for g in hit for d in (0, 1, 2) if (g + d) * lanes < p.shape[0]})
+        sel = np.concatenate([np.arange(g * lanes, min((g + 1) * lanes, p.shape[0])) for g in gs])
+        sub = p[sel]
+        ts = [ref[int(x["idr"]):int(x["idr"]) + int(x["len1"])] for x in sub]
+        qs = [qer[int(x["idq"]):int(x["idq"]) + int(x["len2"])] for x in sub]
+        cp, cr, cq = pack(ts, qs, sub["h0"])
+        yield name, cp, cr, cq, w, bits

@@ -16,7 +16,7 @@ _lib = None
 def build(force=False):
     srcs = [os.path.join(HERE, "emu.cpp"), os.path.join(HERE, "fake", "cuda_runtime.h"),
             os.path.join(CSRC, "bsw_kernel.cuh"), os.path.join(CSRC, "bsw_lane.cuh"),
-            os.path.join(CSRC, "sw_kernel.cuh")]
+            os.path.join(CSRC, "sw_kernel.cuh"), os.path.join(CSRC, "bsw_group.cuh")]
     if force or not os.path.exists(SO) or os.path.getmtime(SO) < max(os.path.getmtime(s) for s in srcs):
         os.makedirs(os.path.dirname(SO), exist_ok=True)
         subprocess.check_call(["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-pthread", "-w",
@@ -46,6 +46,31 @@ def run(pairs, ref, qer, w, params, bits=16, K=4, warps=1, wpair=None, G=32, win
                      ctypes.c_longlong(qer.shape[0]), int(out.shape[0]), int(w),
                      None if wp is None else vp(wp.ctypes.data), int(bits), vp(kp.ctypes.data),
                      int(G), int(K), int(warps), int(win), ctypes.byref(ef), ctypes.byref(ei))
+    return out, ef.value, ei.value
+
+
+def run_group(pairs, ref, qer, w, params, bits=16, warps=2, ref_lo=0, qer_lo=0):
+    """Scores a copy of pairs with the emulated grouped kernel (the
+    reference's groups of 32 / 64 consecutive pairs, one warp each); ref /
+    qer are the windows starting at caller offsets ref_lo / qer_lo.
+    Returns (pairs, err_flags, err_index)."""
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+    out = np.ascontiguousarray(pairs).copy()
+    kp = np.array([params[k] for k in ("o_del", "e_del", "o_ins", "e_ins", "zdrop", "end_bonus", "a", "b")],
+                  np.int32)
+    ef = ctypes.c_int(0)
+    ei = ctypes.c_longlong(0)
+    ref = np.ascontiguousarray(ref)
+    qer = np.ascontiguousarray(qer)
+    vp = ctypes.c_void_p
+    rc = _lib.emu_bsw_group_run(vp(out.ctypes.data), vp(ref.ctypes.data), ctypes.c_longlong(ref_lo),
+                                ctypes.c_longlong(ref_lo + ref.shape[0]), vp(qer.ctypes.data),
+                                ctypes.c_longlong(qer_lo), ctypes.c_longlong(qer_lo + qer.shape[0]),
+                                int(out.shape[0]), int(w), int(bits), vp(kp.ctypes.data), int(warps),
+                                ctypes.byref(ef), ctypes.byref(ei))
+    assert rc == 0, "divergent warp exit"
     return out, ef.value, ei.value
 
 

@@ -21,6 +21,7 @@ std::mutex atomic_mu;
 #include "bsw_lane.cuh"
 #include "sw_kernel.cuh"
 #include "chain_kernel.cuh"
+#include "bsw_group.cuh"
 #include <functional>
 
 // Runs one launch of A (one block of `warps` warps); -1 if a warp's lanes
@@ -28,10 +29,12 @@ std::mutex atomic_mu;
 // sw != nullptr: the unbanded Smith-Waterman kernel with those arguments
 // instead (G, K unused).
 static int sw_packed = 0;  // the unbanded kernel: 1 = two pairs per warp (16x2)
+static const talbsw::GroupArgs *g_group = nullptr;  // set: the grouped kernel instead
 
 static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
                       const talsw::SwArgs *sw = nullptr, const talchain::ChainArgs *ch = nullptr) {
-    size_t wbytes = ch ? talchain::chain_warp_smem_bytes(ch->bw) + 16
+    size_t wbytes = g_group ? 64
+                  : ch ? talchain::chain_warp_smem_bytes(ch->bw) + 16
                   : sw ? (sw_packed ? talsw::sw2_warp_smem_bytes(sw->cols_cap) : talsw::sw_warp_smem_bytes(sw->cols_cap))
                   : G == 1 ? talbsw::lane_warp_smem_bytes(A.cols_cap, A.win)
                            : talbsw::warp_smem_bytes(A.cols_cap, A.rows_cap, G, A.win);
@@ -57,6 +60,7 @@ static int run_launch(talbsw::LaunchArgs &A, int G, int K, int warps,
                 simt::tl_gridDim.x = 1;
                 simt::tl_warp = a.W;
                 simt::tl_smem = a.sm;
+                if (g_group) { if (g_group->bits == 8) talbsw::bsw_group_kernel<8>(*g_group); else talbsw::bsw_group_kernel<16>(*g_group); a.W->done[a.t & 31] = true; return; }
                 if (a.ch) { talchain::chain_kernel(*a.ch); a.W->done[a.t & 31] = true; return; }
                 if (a.sw) { if (sw_packed) talsw::sw_wave2_kernel<talsw::kSwRows>(*a.sw); else talsw::sw_wave_kernel<talsw::kSwRows>(*a.sw); a.W->done[a.t & 31] = true; return; }
                 if (a.G == 1) { const bool sym = a.A->P.o_del == a.A->P.o_ins && a.A->P.e_del == a.A->P.e_ins; int v = a.K == 4 ? 3 : a.K == 2 ? 2 : 1; if (!sym) v &= 1; if (a.A->win > 0 && (a.A->win & (a.A->win - 1))) v |= 4;
@@ -113,6 +117,37 @@ extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long
     A.work_counter = &counter; A.err_flags = err_flags; A.err_index = err_index;
     A.P = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], kp[6], kp[7]};
     return run_launch(A, G, K, warps);
+}
+
+// The grouped kernel (the reference's SIMD groups, one warp each) over n
+// pairs with one band; `warps` warps share the groups.
+extern "C" int emu_bsw_group_run(talbsw::DevPair *pairs, const uint8_t *ref, long long ref_lo,
+                                 long long ref_hi, const uint8_t *qer, long long qer_lo,
+                                 long long qer_hi, int n, int w, int bits, const int32_t *kp,
+                                 int warps, int *err_flags, long long *err_index) {
+    talbsw::GroupArgs G;
+    std::memset(&G, 0, sizeof(G));
+    G.pairs = pairs;
+    G.ref = ref; G.ref_lo = ref_lo; G.ref_hi = ref_hi;
+    G.qer = qer; G.qer_lo = qer_lo; G.qer_hi = qer_hi;
+    G.n = n; G.w = w; G.bits = bits;
+    int m2 = 1;
+    for (int i = 0; i < n; i++) m2 = std::max(m2, pairs[i].len2);
+    G.col_cap = m2 + 3;
+    G.slot_elems = talbsw::group_slot_elems(G.col_cap, bits);
+    std::vector<int16_t> scratch(G.slot_elems * warps, (int16_t)0x5a5a);  // poisoned
+    G.scratch = scratch.data();
+    int counter = 0;
+    unsigned long long cells = 0;
+    *err_flags = 0; *err_index = (long long)INT64_MAX;
+    G.work_counter = &counter; G.cells = &cells; G.err_flags = err_flags; G.err_index = err_index;
+    G.P = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], kp[6], kp[7]};
+    talbsw::LaunchArgs A;
+    std::memset(&A, 0, sizeof(A));
+    g_group = &G;
+    const int rc = run_launch(A, 1, 4, warps);
+    g_group = nullptr;
+    return rc;
 }
 
 // A serving tick: nreq requests, each with its own pair array, sequence

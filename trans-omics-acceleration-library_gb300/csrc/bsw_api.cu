@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "bsw_ctx.h"
+#include "bsw_group.cuh"
 #include "bucket_scan.cuh"
 
 static_assert(sizeof(tal_seq_pair) == 56, "SeqPair is 14 x int32 (bandedSWA.h:90-99)");
@@ -137,6 +138,50 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k, int slot =
     return TAL_OK;
 }
 
+// Grouped scoring (TAL_BSW_GROUPED) of pairs already on the device: one warp
+// per SIMD group of the reference, each with a scratch slot of the group's
+// rows (cols_cap = the longest query), up to 16 warps per SM and 1 GiB of
+// scratch.
+int launch_grouped(tal_bsw_ctx *h, const talbsw::LaunchArgs &A, int slot = 0) {
+    Ctrl *c = reinterpret_cast<Ctrl *>(h->ctrl.p) + slot;
+    talbsw::GroupArgs G;
+    memset(&G, 0, sizeof(G));
+    G.pairs = A.pairs;
+    G.ref = A.ref; G.qer = A.qer;
+    G.ref_lo = A.ref_lo; G.ref_hi = A.ref_hi; G.qer_lo = A.qer_lo; G.qer_hi = A.qer_hi;
+    G.n = A.n;
+    G.w = A.w;
+    G.bits = A.bits;
+    G.col_cap = std::max(A.cols_cap, 1) + 3;
+    G.slot_elems = talbsw::group_slot_elems(G.col_cap, A.bits);
+    G.work_counter = &c->counter;
+    G.err_flags = &c->flags;
+    G.err_index = &c->bad_index;
+    G.cells = &c->cells;
+    G.P = h->kp;
+    const long long ngroups = ((long long)A.n + talbsw::group_lanes(A.bits) - 1) / talbsw::group_lanes(A.bits);
+    const long long slot_bytes = (long long)G.slot_elems * 2;
+    long long warps = std::min<long long>((long long)h->num_sms * 16, ngroups);
+    warps = std::min<long long>(warps, std::max<long long>(4, (1LL << 30) / slot_bytes));
+    const int blocks = (int)((warps + 3) / 4);
+    cudaError_t e = h->gscratch.ensure((size_t)blocks * 4 * (size_t)slot_bytes);
+    if (e != cudaSuccess) return fail(h, TAL_ENOMEM, "grouped scoring scratch");
+    G.scratch = reinterpret_cast<int16_t *>(h->gscratch.p);
+    Ctrl init = {0, 0, (long long)INT64_MAX, 0ull};
+    e = cudaMemcpyAsync(c, &init, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(ctrl)");
+    if (h->kev0) cudaEventRecord(h->kev0, h->stream);
+    if (A.bits == 8)
+        talbsw::bsw_group_kernel<8><<<blocks, 128, 0, h->stream>>>(G);
+    else
+        talbsw::bsw_group_kernel<16><<<blocks, 128, 0, h->stream>>>(G);
+    e = cudaGetLastError();
+    if (h->kev1) cudaEventRecord(h->kev1, h->stream);
+    h->launches++;
+    if (e != cudaSuccess) return cuda_fail(h, e, "grouped kernel launch");
+    return TAL_OK;
+}
+
 // Waits for the launches of control blocks [0, nslots) and merges their
 // status: flags or-ed, the first bad pair (block k's pair indices start at
 // k * per), cells summed.
@@ -229,7 +274,7 @@ int tal_bsw_destroy(tal_bsw_handle h) {
         h->border.release();
         h->porder.release();
         for (DevBuf *b : {&h->xref, &h->xreads, &h->xjobs, &h->xpairs, &h->xtarena, &h->xqarena,
-                          &h->xout})
+                          &h->xout, &h->xretry, &h->gscratch})
             b->release();
         h->bseg.release();
         h->bctrl.release();
@@ -254,7 +299,9 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
     std::lock_guard<std::mutex> lk(h->mu);
     h->last_error.clear();
     h->last_bad = -1;
-    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16))
+    const bool grouped = (bits & TAL_BSW_GROUPED) != 0;
+    bits &= ~TAL_BSW_GROUPED;
+    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16) || (grouped && bits == 0))
         return fail(h, TAL_EINVAL, "bad numPairs or bits");
     if (numPairs == 0) return TAL_OK;
     if (!pairs || !seqBufRef || !seqBufQer) return fail(h, TAL_EINVAL, "NULL buffer");
@@ -273,6 +320,7 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
         if (c >= 1 && c <= kChunks) nch = numPairs >= kChunkMin ? c : 1;
     }
     int32_t per = (numPairs + nch - 1) / nch;
+    if (grouped) per = (per + 63) & ~63;  // chunks end on SIMD-group boundaries
     Ext ext[kChunks];
     auto scan = [&](int c) {
         Ext &x = ext[c];
@@ -318,6 +366,20 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
         if (x.rhi <= x.rlo) x.rhi = x.rlo + 16;
         if (x.qhi <= x.qlo) x.qhi = x.qlo + 16;
     };
+    // grouped 8-bit: the padding lanes of a last partial group read the
+    // query bytes at offset 0 (the reference pads with zeroed SeqPairs)
+    if (grouped && bits == 8 && numPairs % 64) {
+        const long long need = pairs[numPairs - 1].len2;
+        all.qlo = 0;
+        all.qhi = std::max(all.qhi, need);
+        for (int c = 0; c < nch; c++) {
+            const int32_t k1 = std::min<int32_t>(numPairs, (c + 1) * per);
+            if (k1 == numPairs && (int64_t)c * per < numPairs) {
+                ext[c].qlo = 0;
+                ext[c].qhi = std::max(ext[c].qhi, need);
+            }
+        }
+    }
     align(all);
     for (int c = 0; c < nch; c++) align(ext[c]);
     // chunk windows that overlap much (pairs sharing sequences) copy once, whole
@@ -394,7 +456,7 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
         // one row capacity for all chunks: the kernel configuration stays the same
         A.cols_cap = std::max(all.max2, 1);
         A.rows_cap = std::max(all.max1, 1);
-        int rc = launch_scoring(h, A, w, c);
+        int rc = grouped ? launch_grouped(h, A, c) : launch_scoring(h, A, w, c);
         if (rc != TAL_OK) {
             cudaStreamSynchronize(h->stream);
             if (h->cstream) cudaStreamSynchronize(h->cstream);
@@ -511,7 +573,9 @@ int tal_bsw_scores_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t
     std::lock_guard<std::mutex> lk(h->mu);
     h->last_error.clear();
     h->last_bad = -1;
-    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16))
+    const bool grouped = (bits & TAL_BSW_GROUPED) != 0;
+    bits &= ~TAL_BSW_GROUPED;
+    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16) || (grouped && (bits == 0 || d_w)))
         return fail(h, TAL_EINVAL, "bad numPairs or bits");
     if (numPairs == 0) return TAL_OK;
     if (!d_pairs || !d_ref || !d_qer) return fail(h, TAL_EINVAL, "NULL buffer");
@@ -545,7 +609,7 @@ int tal_bsw_scores_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t
     A.bits = bits;
     A.cols_cap = std::max(hc[1], 1);
     A.rows_cap = std::max(hc[0], 1);
-    int rc = launch_scoring(h, A, w);
+    int rc = grouped ? launch_grouped(h, A) : launch_scoring(h, A, w);
     if (rc != TAL_OK) return rc;
     h->pending_status = TAL_OK;
     return TAL_OK;

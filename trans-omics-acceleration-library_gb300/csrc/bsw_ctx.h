@@ -198,9 +198,10 @@ struct tal_bsw_ctx {
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
     talbsw::DevBuf pairs, ref, qer, ctrl, wpair, caps;
+    talbsw::DevBuf gscratch;  // grouped scoring: one row slot per warp
     talbsw::DevBuf porder;  // plain launch: work order by target length, and its buckets
     // seed extension: reference, reads, copy jobs + seeds, pairs, arenas, regions
-    talbsw::DevBuf xref, xreads, xjobs, xpairs, xtarena, xqarena, xout;
+    talbsw::DevBuf xref, xreads, xjobs, xpairs, xtarena, xqarena, xout, xretry;
     // host-buffer calls in chunks: copies on cstream, chunk k's scoring waits on cev[k]
     cudaStream_t cstream = nullptr;
     cudaEvent_t cev[4] = {};

@@ -1,0 +1,431 @@
+// The reference's SIMD grouping on a warp: getScores16 / getScores8 score
+// their pairs in groups of 32 (16-bit) / 64 (8-bit) consecutive pairs, one
+// pair per vector lane (AVX-512BW widths, bandedSWA.h:66-67), and every group
+// shares one band [beg, end) per row, computed from all of its lanes
+// (bandedSWA.cpp:3080-3316 for 16-bit, :2371-2621 for 8-bit).  A lane's
+// outputs can depend on the other lanes of its group through that shared
+// band: cells outside the lane's own band but inside the group's are still
+// evaluated (masked), which zeroes the lane's row entries there, and the
+// lane's head / tail re-derivation scans from the group's band edges, so a
+// stale non-zero entry past the lane's own end can keep its tail from
+// narrowing.  The per-pair kernels score each pair as if it were alone in its
+// group, which gives the same outputs on almost all inputs; this kernel gives
+// the grouped outputs exactly, for callers that need bit-equality with the
+// reference on any input.
+//
+// One warp is one group: lane l of the group is thread l (16-bit) or threads
+// l and l + 32 share a thread (8-bit, two lanes per thread).  Every value is
+// kept in the element width the reference computes in (int16 / int8, all
+// arithmetic wrapping), so nothing here depends on an exact-range argument.
+// The group's row entries (H, F and the query codes) live in a per-warp slot
+// of global scratch, column-major with the group's lanes contiguous (one
+// column of the group = 64 or 128 bytes, coalesced).
+#pragma once
+
+#include "bsw_kernel.cuh"
+
+namespace talbsw {
+
+struct GroupArgs {
+    DevPair *pairs;
+    const uint8_t *ref, *qer;
+    long long ref_lo, ref_hi, qer_lo, qer_hi;
+    int n;            // pairs; groups = ceil(n / lanes)
+    int w;            // the call's band
+    int bits;         // 8 or 16
+    int col_cap;      // columns of a scratch slot (>= max len2 + 3)
+    int16_t *scratch; // per warp: H[col_cap][lanes], F[col_cap][lanes], then codes
+    size_t slot_elems;  // int16 elements per warp slot
+    int *work_counter;
+    unsigned long long *cells;
+    int *err_flags;
+    long long *err_index;
+    KernelParams P;
+};
+
+// Lanes per group: 64 for 8-bit, 32 for 16-bit (AVX-512BW SIMD_WIDTH8/16).
+__host__ __device__ inline int group_lanes(int bits) { return bits == 8 ? 64 : 32; }
+
+// int16 elements of one warp's scratch slot: H and F (int16 each) and the
+// query codes (one byte each, packed two to an element).
+__host__ __device__ inline size_t group_slot_elems(int col_cap, int bits) {
+    const size_t l = (size_t)group_lanes(bits);
+    return (size_t)col_cap * l * 2 + ((size_t)col_cap * l + 1) / 2 + 8;
+}
+
+__host__ __device__ __forceinline__ unsigned umin(unsigned a, unsigned b) { return a < b ? a : b; }
+__host__ __device__ __forceinline__ unsigned umax(unsigned a, unsigned b) { return a > b ? a : b; }
+
+// Element-width helpers: S = 16 or 8 bits; values are held sign-extended.
+template <int SB>
+struct GE {
+    static constexpr int SH = 32 - SB;
+    static constexpr unsigned MSK = (1u << SB) - 1u;
+    __device__ __forceinline__ static int ws(int x) { return (int)((unsigned)x << SH) >> SH; }
+    __device__ __forceinline__ static unsigned us(int x) { return (unsigned)x & MSK; }
+};
+
+template <int SB>
+__global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
+    typedef GE<SB> E;
+    constexpr int LPT = SB == 8 ? 2 : 1;  // lanes per thread
+    constexpr int W = 32 * LPT;           // lanes per group
+    constexpr bool is16 = SB == 16;
+    const unsigned full = 0xffffffffu;
+    const int t = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int16_t *Hh = A.scratch + (size_t)gw * A.slot_elems;
+    int16_t *Fv = Hh + (size_t)A.col_cap * W;
+    int8_t *Q2 = reinterpret_cast<int8_t *>(Fv + (size_t)A.col_cap * W);
+    const KernelParams &P = A.P;
+    const int ngroups = (A.n + W - 1) / W;
+
+    // scores and constants (bandedSWA.cpp:50-68), wrapped to the element width
+    const int w_match = E::ws((int8_t)P.a);
+    const int w_mismatch = E::ws((int8_t)(P.b * -1));
+    const int e_del = E::ws(P.e_del), oe_del = E::ws(P.o_del + P.e_del);
+    const int e_ins = E::ws(P.e_ins), oe_ins = E::ws(P.o_ins + P.e_ins);
+    const int o_del = E::ws(P.o_del);
+    const int zdropv = E::ws(P.zdrop);
+    int maxsc = 0;  // max of the scores (:2779 / :2082)
+    if (maxsc < (int8_t)P.a) maxsc = E::ws((int8_t)P.a);
+    if (maxsc < (int8_t)(P.b * -1)) maxsc = E::ws((int8_t)(P.b * -1));
+
+    for (;;) {
+        int g = 0;
+        if (t == 0) g = atomicAdd(A.work_counter, 1);
+        g = __shfl_sync(full, g, 0);
+        if (g >= ngroups) break;
+
+        // ---- the group's lanes; lanes past n are padded the way the
+        // reference pads its array (16-bit: len1 = len2 = 0, :2711-2717;
+        // 8-bit: len1 = 0, len2 = the last pair's len2, :2012-2018), h0 = 0
+        int len1[LPT], len2[LPT], h0r[LPT];
+        long long idr[LPT], idq[LPT];
+        bool real[LPT];
+        bool bad = false;
+        for (int u = 0; u < LPT; u++) {
+            const long long k = (long long)g * W + t + 32 * u;
+            real[u] = k < A.n;
+            if (real[u]) {
+                const DevPair &p = A.pairs[k];
+                len1[u] = p.len1; len2[u] = p.len2; h0r[u] = p.h0;
+                idr[u] = p.idr; idq[u] = p.idq;
+                const int lim = is16 ? 32767 : 127;
+                const bool ok = len1[u] >= 0 && len2[u] >= 0 && len1[u] <= lim && len2[u] <= lim &&
+                                h0r[u] >= 0 && idr[u] >= A.ref_lo && idr[u] + len1[u] <= A.ref_hi &&
+                                idq[u] >= A.qer_lo && idq[u] + len2[u] <= A.qer_hi &&
+                                len2[u] + 3 <= A.col_cap;
+                if (!ok) {
+                    atomicOr(A.err_flags, ERR_DOMAIN);
+                    atomicMin(A.err_index, k);
+                    bad = true;
+                }
+            } else {
+                len1[u] = 0;
+                len2[u] = is16 ? 0 : A.pairs[A.n - 1].len2;
+                h0r[u] = 0;
+                idr[u] = idq[u] = -1;
+            }
+        }
+        if (__any_sync(full, bad)) continue;
+
+        // ---- lengths as the wrapper hands them to the kernel
+        int m1 = 0, m2 = 0, mq = 0x7fffffff;
+        for (int u = 0; u < LPT; u++) {
+            m1 = imax(m1, len1[u]);
+            m2 = imax(m2, len2[u]);
+            mq = imin(mq, len2[u]);
+        }
+        const int maxLen1 = __reduce_max_sync(full, m1);
+        const int maxLen2 = __reduce_max_sync(full, m2);
+        const int minq = __reduce_min_sync(full, mq) - 1;
+        const int nrow = maxLen1, ncol = maxLen2, wrapRows = maxLen1;
+        const int colCap = (ncol > 1 ? ncol : 1) + 3;
+
+        // ---- per-lane set-up: query codes, the first row, band clamp
+        int h0[LPT], tlen[LPT], qlen[LPT], myband[LPT];
+        int bsz = A.w;
+        for (int u = 0; u < LPT; u++) {
+            const int l = t + 32 * u;
+            h0[u] = E::ws((int)E::us(h0r[u]));
+            tlen[u] = E::ws((int)E::us(len1[u]));
+            qlen[u] = E::ws((int)E::us(len2[u]));
+            // a padding lane (8-bit) reads the query bytes at the caller's
+            // offset 0, as the reference's zeroed SeqPair does; they only
+            // matter where its wrapped first column is non-zero
+            const uint8_t *q = real[u] ? A.qer + (idq[u] - A.qer_lo)
+                             : (A.qer_lo <= 0 && len2[u] <= A.qer_hi) ? A.qer - A.qer_lo : nullptr;
+            int tt = (h0[u] > oe_ins) ? E::ws(h0[u] - oe_ins) : 0;
+            for (int k = 0; k < colCap; k++) {
+                int code = 0;
+                if (k < len2[u]) {
+                    const int b = q ? q[k] : 4;
+                    if (b > 4 && real[u]) {
+                        atomicOr(A.err_flags, ERR_BASE);
+                        atomicMin(A.err_index, (long long)g * W + l);
+                        bad = true;
+                    }
+                    code = b == 4 ? -1 : E::ws(b);
+                } else if (k <= maxLen2) {
+                    code = 100;  // DUMMY2 (:46)
+                }
+                Q2[(size_t)k * W + l] = (int8_t)code;
+                int hv = 0;
+                if (k == 0) hv = h0[u];
+                else if (k == 1) hv = tt;
+                else if (k < maxLen2) { tt = E::ws(tt - e_ins); tt = tt > 0 ? tt : 0; hv = tt; }
+                Hh[(size_t)k * W + l] = (int16_t)hv;
+                Fv[(size_t)k * W + l] = 0;
+            }
+            // band clamp (:2882-2904 / :2183-2205): integer division, then +1.0
+            const int qlenb = E::ws(len2[u] * maxsc);
+            const int eb_ins = E::ws(P.end_bonus - P.o_ins), eb_del = E::ws(P.end_bonus - P.o_del);
+            int temp = (int)E::us(qlenb + eb_ins);
+            int mi = temp / P.e_ins + 1;
+            mi = mi > 1 ? mi : 1;
+            myband[u] = E::ws((int)E::us(A.w > mi ? mi : A.w));
+            temp = (int)E::us(qlenb + eb_del);
+            mi = temp / P.e_del + 1;
+            mi = mi > 1 ? mi : 1;
+            const int mb = (int)E::us(myband[u]);
+            myband[u] = E::ws((int)E::us(mb > mi ? mi : mb));
+            bsz = imax(bsz, (int)E::us(myband[u]));
+        }
+        if (__any_sync(full, bad)) continue;
+        const int w = __reduce_max_sync(full, bsz);
+        __syncwarp();
+
+        // ---- the kernel proper (:2962-3356 / :2263-2661)
+        int head[LPT], tail[LPT], mlen[LPT], maxScore[LPT], x[LPT], y[LPT], gscore[LPT];
+        int max_off[LPT], exit0[LPT], max_ie[LPT];
+        for (int u = 0; u < LPT; u++) {
+            tail[u] = qlen[u];
+            head[u] = 0;
+            const unsigned ml = E::us(qlen[u] + myband[u]);
+            mlen[u] = E::ws((int)umin(ml, E::us(tlen[u])));
+            maxScore[u] = h0[u];
+            x[u] = y[u] = 0;
+            gscore[u] = -1;
+            max_off[u] = 0;
+            exit0[u] = -1;
+            max_ie[u] = 0;
+        }
+        auto HH = [&](int c, int u) -> int16_t & { return Hh[(size_t)c * W + t + 32 * u]; };
+        auto FF = [&](int c, int u) -> int16_t & { return Fv[(size_t)c * W + t + 32 * u]; };
+        // first column H_v[k]: h0 at k = 0, max(h0 - o_del - k e_del, 0) below
+        // (wrapping), DUMMY1 at the wrapper's last row
+        auto Hv = [&](int k, int u) -> int {
+            if (k == 0) return h0[u];
+            if (k < wrapRows) {
+                const int v = E::ws(h0[u] - o_del - k * e_del);
+                return v > 0 ? v : 0;
+            }
+            return 99;  // DUMMY1 (:45)
+        };
+        unsigned long long ncells = 0;
+        int beg = 0, end = ncol, nbeg = 0, nend = ncol;
+        for (int i = 0; i < nrow; i++) {
+            const int i1 = E::ws(i + 1);
+            int e11[LPT], h10[LPT], maxRS1[LPT], y1[LPT], s1[LPT];
+            beg = nbeg; end = nend;
+            if (beg < i - w) beg = i - w;
+            if (end > i + w + 1) end = i + w + 1;
+            if (end > ncol) end = ncol;
+            bool changed = false;
+            for (int u = 0; u < LPT; u++) {
+                e11[u] = 0; maxRS1[u] = 0; y1[u] = 0;
+                h10[u] = beg == 0 ? Hv(i + 1, u) : 0;
+                if (i < len1[u]) {
+                    const int b = A.ref[idr[u] - A.ref_lo + i];
+                    s1[u] = b == 4 ? -1 : E::ws(b);
+                    if (b > 4) {
+                        atomicOr(A.err_flags, ERR_BASE);
+                        atomicMin(A.err_index, (long long)g * W + t + 32 * u);
+                    }
+                } else {
+                    s1[u] = 99;  // DUMMY1
+                }
+                // per-lane band (:3080-3089)
+                const int ph = head[u], pt = tail[u];
+                const int c = E::ws(i - myband[u]);
+                head[u] = head[u] > c ? head[u] : c;
+                unsigned tu = umin(E::us(tail[u]), E::us(i1 + myband[u]));
+                tu = umin(tu, E::us(qlen[u]));
+                tail[u] = E::ws((int)tu);
+                changed |= head[u] != ph || tail[u] != pt;
+            }
+            // trimming (:3091-3112)
+            if (__any_sync(full, changed)) {
+                for (int lc = beg; lc < end; lc++) {
+                    const int pj = E::ws(lc), jn = E::ws(lc + 1);
+                    bool any = false;
+                    for (int u = 0; u < LPT; u++) any |= head[u] > pj;
+                    if (!__any_sync(full, any)) break;
+                    for (int u = 0; u < LPT; u++)
+                        if (head[u] > pj || jn > tail[u]) { HH(lc, u) = 0; FF(lc, u) = 0; }
+                }
+            }
+            // row exit status (:3119-3129)
+            for (int u = 0; u < LPT; u++)
+                if (i1 > mlen[u] || tail[u] == head[u] || head[u] > tail[u]) exit0[u] = 0;
+
+            // DP row (:3135-3196)
+            int j512 = E::ws(beg);
+            int j;
+            for (j = beg; j < end; j++) {
+                const int pj = j512;
+                j512 = E::ws(j512 + 1);
+#pragma unroll
+                for (int u = 0; u < LPT; u++) {
+                    const int h00 = HH(j, u), f11 = FF(j, u);
+                    const int a2 = Q2[(size_t)j * W + t + 32 * u];
+                    int sbt = s1[u] == a2 ? w_match : w_mismatch;
+                    // the larger code's top bit (as unsigned): an N on either side
+                    if (umax(E::us(s1[u]), E::us(a2)) > (E::MSK >> 1)) sbt = -1;
+                    int m11 = E::ws(h00 + sbt);
+                    if (h00 == 0) m11 = 0;
+                    int h11 = m11 > e11[u] ? m11 : e11[u];
+                    h11 = h11 > f11 ? h11 : f11;
+                    int tv = E::ws(m11 - oe_ins);
+                    int val = tv > 0 ? tv : 0;
+                    const int ee = E::ws(e11[u] - e_ins);
+                    e11[u] = val > ee ? val : ee;
+                    tv = E::ws(m11 - oe_del);
+                    val = tv > 0 ? tv : 0;
+                    int f21 = E::ws(f11 - e_del);
+                    f21 = val > f21 ? val : f21;
+                    const bool cmp2 = head[u] > pj;
+                    const bool mask = pj > tail[u] || cmp2;
+                    const int hst = mask ? 0 : h10[u];
+                    if (mask) f21 = 0;
+                    const int bmax = maxRS1[u];
+                    const int nm = maxRS1[u] > h11 ? maxRS1[u] : h11;
+                    const bool cmpA = nm > bmax || nm == h11;
+                    if (!(j512 > tail[u] || cmp2)) {
+                        if (cmpA) y1[u] = j512;
+                        maxRS1[u] = nm;
+                    }
+                    FF(j, u) = (int16_t)f21;
+                    HH(j, u) = (int16_t)hst;
+                    h10[u] = h11;
+                    if (j >= minq) {
+                        const bool cq = j512 == qlen[u];
+                        int max_gh = gscore[u] > h11 ? gscore[u] : h11;
+                        int t1 = gscore[u] > h11 ? max_ie[u] : i1;
+                        t1 = cq ? t1 : max_ie[u];
+                        const bool mex0 = exit0[u] < 0;
+                        t1 = mex0 ? t1 : max_ie[u];
+                        max_gh = mex0 ? max_gh : gscore[u];
+                        max_gh = cq ? max_gh : gscore[u];
+                        const bool ct = j512 > tail[u];
+                        max_gh = ct ? gscore[u] : max_gh;
+                        max_ie[u] = ct ? max_ie[u] : t1;
+                        gscore[u] = max_gh;
+                    }
+                }
+            }
+            if (end > beg) ncells += (unsigned long long)(end - beg);
+            // the row's last column (:3197-3203); j == max(beg, end) here
+            if (j < colCap) {
+                for (int u = 0; u < LPT; u++) {
+                    const bool m = head[u] > j512 || j512 > tail[u];
+                    HH(j, u) = (int16_t)(m ? 0 : h10[u]);
+                    FF(j, u) = 0;
+                }
+            }
+            // a zero row in every lane ends the group (:3206-3209)
+            bool nz = false;
+            for (int u = 0; u < LPT; u++) nz |= maxRS1[u] != 0;
+            if (!__any_sync(full, nz)) break;
+            for (int u = 0; u < LPT; u++) {
+                if (maxRS1[u] == 0) exit0[u] = 0;
+                const int bms = maxScore[u];
+                const int sc2 = maxScore[u] > maxRS1[u] ? maxScore[u] : maxRS1[u];
+                if (exit0[u] < 0) maxScore[u] = sc2;
+                if (maxScore[u] > bms) {
+                    y[u] = y1[u];
+                    x[u] = i1;
+                    int ind = E::ws(y1[u] - i1);
+                    ind = ind < 0 ? E::ws(-ind) : ind;  // abs (wrapping)
+                    max_off[u] = max_off[u] > ind ? max_off[u] : ind;
+                }
+                // ZSCORE16 / ZSCORE8 (:1868-1881 / :1826-1839)
+                const int tmpi = E::ws(i1 - x[u]), tmpj = E::ws(y1[u] - y[u]);
+                const int score = E::ws(maxScore[u] - maxRS1[u]);
+                const int d = tmpi > tmpj ? E::ws(tmpi - tmpj) : E::ws(tmpj - tmpi);
+                if (E::ws(score - d) > zdropv) exit0[u] = 0;
+            }
+            // band narrowing (:3235-3260): columns zero in every lane
+            auto all_zero = [&](int c) {
+                bool z = true;
+                for (int u = 0; u < LPT; u++) z &= (HH(c, u) | FF(c, u)) == 0;
+                return __all_sync(full, z) != 0;
+            };
+            int lc;
+            for (lc = beg; lc < end; lc++) {
+                if (all_zero(lc)) nbeg = lc;
+                else break;
+            }
+            for (lc = end; lc >= beg; lc--)
+                if (!all_zero(lc)) break;
+            nend = lc + 2 < ncol ? lc + 2 : ncol;
+            if (is16) { beg = nbeg; end = nend; }
+            // per-lane head / tail (:3265-3316 / :2571-2621)
+            {
+                bool run[LPT];
+                auto zero_at = [&](int c, int u) {
+                    return exit0[u] != 0 && (HH(c, u) | FF(c, u)) == 0;
+                };
+                for (int u = 0; u < LPT; u++) run[u] = true;
+                int l512 = E::ws(beg);
+                for (lc = beg; lc < end; lc++) {
+                    bool zl[LPT], any = false;
+                    for (int u = 0; u < LPT; u++) { zl[u] = zero_at(lc, u); any |= zl[u]; }
+                    if (!__any_sync(full, any)) break;
+                    l512 = E::ws(l512 + 1);
+                    for (int u = 0; u < LPT; u++) {
+                        run[u] = zl[u] && run[u];
+                        if (run[u]) head[u] = l512;
+                    }
+                }
+                int index[LPT];
+                for (int u = 0; u < LPT; u++) { index[u] = tail[u]; run[u] = true; }
+                l512 = E::ws(end);
+                for (lc = end; lc >= beg; lc--) {
+                    bool zl[LPT], any = false;
+                    for (int u = 0; u < LPT; u++) { zl[u] = zero_at(lc, u); any |= zl[u]; }
+                    if (!__any_sync(full, any)) break;
+                    l512 = E::ws(l512 - 1);
+                    for (int u = 0; u < LPT; u++) {
+                        run[u] = zl[u] && run[u];
+                        if (run[u]) index[u] = l512;
+                    }
+                }
+                for (int u = 0; u < LPT; u++) {
+                    const int ix = E::ws(index[u] + 2);
+                    tail[u] = ix < qlen[u] ? ix : qlen[u];
+                }
+            }
+            __syncwarp();
+        }
+        for (int u = 0; u < LPT; u++) {
+            if (!real[u]) continue;
+            DevPair &p = A.pairs[(long long)g * W + t + 32 * u];
+            p.score = maxScore[u];
+            p.tle = x[u];
+            p.qle = y[u];
+            p.max_off = max_off[u];
+            p.gscore = gscore[u];
+            p.gtle = max_ie[u];
+        }
+        if (t == 0 && A.cells) {
+            int nreal = A.n - g * W;
+            nreal = nreal < W ? nreal : W;
+            atomicAdd(A.cells, ncells * (unsigned long long)nreal);
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace talbsw

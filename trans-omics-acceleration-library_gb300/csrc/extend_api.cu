@@ -140,7 +140,8 @@ extern "C" int tal_bsw_extend_seeds(tal_bsw_handle h, const uint8_t *ref, int64_
     if (!h) return TAL_EINVAL;
     h->last_error.clear();
     h->last_bad = -1;
-    if (!xp || n_reads < 0 || n_seeds < 0 || ref_len < 0 || xp->w < 0)
+    if (!xp || n_reads < 0 || n_seeds < 0 || ref_len < 0 || xp->w < 0 || xp->band_tries < 0 ||
+        xp->band_tries > 8 || ((long long)xp->w << std::max(0, xp->band_tries - 1)) > (1LL << 24))
         return xfail(h, TAL_EINVAL, "bad counts or parameters");
     if (n_seeds == 0) return TAL_OK;
     if (!ref || !reads || !read_off || !seeds || !out) return xfail(h, TAL_EINVAL, "NULL buffer");
@@ -246,28 +247,73 @@ extern "C" int tal_bsw_extend_seeds(tal_bsw_handle h, const uint8_t *ref, int64_
         h->launches++;
     }
     const int gb = (int)std::min<long long>(((long long)n_seeds + 255) / 256, 8LL * h->num_sms);
-    int rc;
-    // left batch, then the right batch's h0 from its results, then the right batch
-    if (!lp.empty()) {
-        rc = tal_bsw_scores_device(h, d_lp, d_t, (size_t)tpos + 16, d_q, (size_t)qpos + 16,
-                                   (int32_t)lp.size(), xp->w, nullptr, TAL_BSW_AUTO);
+    const int tries = std::max(1, xp->band_tries);
+    // One extension batch on the device (its pairs at d_p, host copy hp for
+    // the seed ids), with the band retries: pairs whose attempt wants another
+    // go again, as a sub-batch, with the doubled band.
+    auto run_batch = [&](tal_seq_pair *d_p, std::vector<tal_seq_pair> &hp) -> int {
+        const int32_t n = (int32_t)hp.size();
+        int rc = tal_bsw_scores_device(h, d_p, d_t, (size_t)tpos + 16, d_q, (size_t)qpos + 16, n, xp->w,
+                                       nullptr, TAL_BSW_AUTO);
         if (rc == TAL_OK) rc = tal_bsw_sync(h);
         if (rc != TAL_OK) {
-            if (h->last_bad >= 0) h->last_bad = lp[(size_t)h->last_bad].id;
+            if (h->last_bad >= 0) h->last_bad = hp[(size_t)h->last_bad].id;
             return rc;
         }
-    }
+        if (tries <= 1) return TAL_OK;
+        cudaError_t e2 = cudaMemcpyAsync(hp.data(), d_p, pb * n, cudaMemcpyDeviceToHost, s);
+        if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(s);
+        if (e2 != cudaSuccess) return xfail(h, TAL_ECUDA, cudaGetErrorString(e2));
+        // prev: the score before the pair's last attempt; idx: the pairs still
+        // retrying (all of them before the first check)
+        std::vector<int32_t> prev((size_t)n, -1), idx((size_t)n), cur;
+        for (int32_t k = 0; k < n; k++) idx[k] = k;
+        std::vector<tal_seq_pair> sub;
+        for (int i = 1; i < tries; i++) {
+            const int wprev = xp->w << (i - 1);
+            cur.clear();
+            sub.clear();
+            for (int32_t k : idx) {
+                const tal_seq_pair &p = hp[k];
+                if (p.score != prev[k] && p.max_off >= (wprev >> 1) + (wprev >> 2)) {
+                    cur.push_back(k);
+                    prev[k] = p.score;
+                    tal_seq_pair q = p;
+                    q.score = q.tle = q.gtle = q.qle = q.gscore = q.max_off = -1;
+                    sub.push_back(q);
+                }
+            }
+            idx.swap(cur);
+            if (idx.empty()) break;
+            if (h->xretry.ensure(pb * sub.size()) != cudaSuccess)
+                return xfail(h, TAL_ENOMEM, "band retry buffer");
+            tal_seq_pair *d_r = reinterpret_cast<tal_seq_pair *>(h->xretry.p);
+            e2 = cudaMemcpyAsync(d_r, sub.data(), pb * sub.size(), cudaMemcpyHostToDevice, s);
+            if (e2 != cudaSuccess) return xfail(h, TAL_ECUDA, cudaGetErrorString(e2));
+            rc = tal_bsw_scores_device(h, d_r, d_t, (size_t)tpos + 16, d_q, (size_t)qpos + 16,
+                                       (int32_t)sub.size(), xp->w << i, nullptr, TAL_BSW_AUTO);
+            if (rc == TAL_OK) rc = tal_bsw_sync(h);
+            if (rc != TAL_OK) {
+                if (h->last_bad >= 0) h->last_bad = sub[(size_t)h->last_bad].id;
+                return rc;
+            }
+            e2 = cudaMemcpyAsync(sub.data(), d_r, pb * sub.size(), cudaMemcpyDeviceToHost, s);
+            if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(s);
+            if (e2 != cudaSuccess) return xfail(h, TAL_ECUDA, cudaGetErrorString(e2));
+            for (size_t m = 0; m < idx.size(); m++) hp[idx[m]] = sub[m];
+        }
+        e2 = cudaMemcpyAsync(d_p, hp.data(), pb * n, cudaMemcpyHostToDevice, s);
+        if (e2 != cudaSuccess) return xfail(h, TAL_ECUDA, cudaGetErrorString(e2));
+        return TAL_OK;
+    };
+    int rc;
+    // left batch, then the right batch's h0 from its results, then the right batch
+    if (!lp.empty() && (rc = run_batch(d_lp, lp)) != TAL_OK) return rc;
     if (!rp.empty()) {
         right_h0_kernel<<<gb, 256, 0, s>>>(d_xs, n_seeds, reinterpret_cast<const talbsw::DevPair *>(d_lp),
                                            reinterpret_cast<talbsw::DevPair *>(d_rp), a, xp->pen_clip5);
         h->launches++;
-        rc = tal_bsw_scores_device(h, d_rp, d_t, (size_t)tpos + 16, d_q, (size_t)qpos + 16,
-                                   (int32_t)rp.size(), xp->w, nullptr, TAL_BSW_AUTO);
-        if (rc == TAL_OK) rc = tal_bsw_sync(h);
-        if (rc != TAL_OK) {
-            if (h->last_bad >= 0) h->last_bad = rp[(size_t)h->last_bad].id;
-            return rc;
-        }
+        if ((rc = run_batch(d_rp, rp)) != TAL_OK) return rc;
     }
     finalize_kernel<<<gb, 256, 0, s>>>(d_xs, n_seeds, reinterpret_cast<const talbsw::DevPair *>(d_lp),
                                        reinterpret_cast<const talbsw::DevPair *>(d_rp), a, xp->pen_clip5,

@@ -25,6 +25,7 @@ TAL_OK, TAL_EINVAL, TAL_EDOMAIN, TAL_ENOMEM, TAL_ECUDA, TAL_ETIMEOUT, TAL_ENODEV
 STATUS_NAMES = {0: "TAL_OK", 1: "TAL_EINVAL", 2: "TAL_EDOMAIN", 3: "TAL_ENOMEM", 4: "TAL_ECUDA",
                 5: "TAL_ETIMEOUT", 6: "TAL_ENODEV", 7: "TAL_EBUSY"}
 AUTO, BITS8, BITS16 = 0, 8, 16
+GROUPED = 0x100  # OR into BITS8 / BITS16: the reference's SIMD groups, exactly
 
 
 class TalBswError(RuntimeError):
@@ -157,12 +158,16 @@ class BandedPairWiseSW:
 
     # -- reference entry points -------------------------------------------------
     def getScores8(self, pairArray, seqBufRef, seqBufQer, numPairs: int, numThreads: int = 1,
-                   w: int = 100) -> None:
-        self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, BITS8)
+                   w: int = 100, grouped: bool = False) -> None:
+        """grouped: score in the reference's groups of 64 consecutive pairs
+        (equal to the reference's outputs on any input; slower)."""
+        self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, BITS8 | (GROUPED if grouped else 0))
 
     def getScores16(self, pairArray, seqBufRef, seqBufQer, numPairs: int, numThreads: int = 1,
-                    w: int = 100) -> None:
-        self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, BITS16)
+                    w: int = 100, grouped: bool = False) -> None:
+        """grouped: score in the reference's groups of 32 consecutive pairs
+        (equal to the reference's outputs on any input; slower)."""
+        self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, BITS16 | (GROUPED if grouped else 0))
 
     def getScoresAuto(self, pairArray, seqBufRef, seqBufQer, numPairs: int,
                       numThreads: int = 1, w: int = 100) -> None:
