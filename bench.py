@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling)")
     ap.add_argument("--pairs", type=int, default=None,
                     help="score only the first N pairs of the workload (profiling a small case)")
+    ap.add_argument("--no-grouped", action="store_true",
+                    help="skip the grouped-form (TAL_BSW_GROUPED) leg")
     ap.add_argument("--no-mixed", action="store_true",
                     help="skip the mixed-length plain-vs-batched comparison")
     ap.add_argument("--mixed-pairs", type=int, default=None,
@@ -399,6 +401,38 @@ def run_ours(args):
                        "graph); segments: [lanes per pair, columns per lane, max query, row ring]; "
                        "wall time per synchronous call"}
 
+    # ---- grouped form (the reference's SIMD groups, exact on any input) on
+    # the same pairs: its speed, and how many pairs' outputs differ from the
+    # per-pair kernels' (pairs whose outputs depend on their group)
+    grouped = None
+    if not args.no_grouped:
+        log("grouped form")
+        gbits = bits | tal_bsw.api.GROUPED
+
+        def step_grouped():
+            bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                              n, wl.w, gbits)
+        step_grouped()
+        gout = dp.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE)
+        ndiff = int((tal_bsw.outputs(gout) != tal_bsw.outputs(dev_out)).any(1).sum())
+        gsteps = 2
+        dist.barrier()
+        torch.cuda.synchronize()
+        g0 = time.perf_counter()
+        gk = 0.0
+        for _ in range(gsteps):
+            step_grouped()
+            gk += bsw.last_kernel_ms
+        torch.cuda.synchronize()
+        t_grouped = dist.max((time.perf_counter() - g0) / gsteps)
+        grouped = {"value": round(total_cells / t_grouped / 1e9, 3), "unit": UNIT,
+                   "ms_per_step": round(t_grouped * 1e3, 3),
+                   "kernel_ms_per_launch": round(gk / gsteps, 3),
+                   "pairs_differing_from_per_pair": dist.sum(ndiff),
+                   "note": "device-resident call with TAL_BSW_GROUPED (one warp per SIMD group of "
+                           "the reference, wrapping int16/int8 values); wall time per synchronous "
+                           "call"}
+
     # ---- rooflines
     hbm_peak, peak_src = measured_peaks()
     alg_bytes = lens + 56 * n + 24 * n          # bases read, SeqPair read, outputs written
@@ -438,6 +472,8 @@ def run_ours(args):
         "clocks": clk,
         "batched": batched,
     }
+    if grouped:
+        result["grouped"] = grouped
     if not args.no_mixed:
         log("mixed-length plain vs batched")
         result["mixed"] = run_mixed(args, bsw, dist)
