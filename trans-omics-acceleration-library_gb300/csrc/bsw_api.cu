@@ -140,8 +140,8 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k, int slot =
 
 // Grouped scoring (TAL_BSW_GROUPED) of pairs already on the device: one warp
 // per SIMD group of the reference, each with a scratch slot of the group's
-// rows (cols_cap = the longest query), up to 16 warps per SM and 1 GiB of
-// scratch.
+// rows (cols_cap = the longest query), up to 48 warps per SM (as many as
+// fit) and 1 GiB of scratch.
 int launch_grouped(tal_bsw_ctx *h, const talbsw::LaunchArgs &A, int slot = 0) {
     Ctrl *c = reinterpret_cast<Ctrl *>(h->ctrl.p) + slot;
     talbsw::GroupArgs G;
@@ -161,7 +161,9 @@ int launch_grouped(tal_bsw_ctx *h, const talbsw::LaunchArgs &A, int slot = 0) {
     G.P = h->kp;
     const long long ngroups = ((long long)A.n + talbsw::group_lanes(A.bits) - 1) / talbsw::group_lanes(A.bits);
     const long long slot_bytes = (long long)G.slot_elems * 2;
-    long long warps = std::min<long long>((long long)h->num_sms * 16, ngroups);
+    int wps = 48;  // warps per SM (tuning: TAL_BSW_GROUP_WARPS; 16 / 32 / 48 measured 97 / 108 / 121 GCUPS on C2)
+    if (const char *ev = getenv("TAL_BSW_GROUP_WARPS")) wps = std::min(std::max(atoi(ev), 4), 64);
+    long long warps = std::min<long long>((long long)h->num_sms * wps, ngroups);
     warps = std::min<long long>(warps, std::max<long long>(4, (1LL << 30) / slot_bytes));
     const int blocks = (int)((warps + 3) / 4);
     cudaError_t e = h->gscratch.ensure((size_t)blocks * 4 * (size_t)slot_bytes);

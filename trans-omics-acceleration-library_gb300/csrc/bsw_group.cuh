@@ -17,9 +17,9 @@
 // l and l + 32 share a thread (8-bit, two lanes per thread).  Every value is
 // kept in the element width the reference computes in (int16 / int8, all
 // arithmetic wrapping), so nothing here depends on an exact-range argument.
-// The group's row entries (H, F and the query codes) live in a per-warp slot
-// of global scratch, column-major with the group's lanes contiguous (one
-// column of the group = 64 or 128 bytes, coalesced).
+// The group's row entries (H and F packed in one word, and the query codes)
+// live in a per-warp slot of global scratch, column-major with the group's
+// lanes contiguous (one column of the group = 128 or 256 bytes, coalesced).
 #pragma once
 
 #include "bsw_kernel.cuh"
@@ -34,7 +34,7 @@ struct GroupArgs {
     int w;            // the call's band
     int bits;         // 8 or 16
     int col_cap;      // columns of a scratch slot (>= max len2 + 3)
-    int16_t *scratch; // per warp: H[col_cap][lanes], F[col_cap][lanes], then codes
+    int16_t *scratch; // per warp: (H, F) words [col_cap][lanes], then the codes
     size_t slot_elems;  // int16 elements per warp slot
     int *work_counter;
     unsigned long long *cells;
@@ -46,11 +46,14 @@ struct GroupArgs {
 // Lanes per group: 64 for 8-bit, 32 for 16-bit (AVX-512BW SIMD_WIDTH8/16).
 __host__ __device__ inline int group_lanes(int bits) { return bits == 8 ? 64 : 32; }
 
-// int16 elements of one warp's scratch slot: H and F (int16 each) and the
-// query codes (one byte each, packed two to an element).
+// int16 elements of one warp's scratch slot: H and F (int16 each, one word
+// per lane and column) and the query codes (one byte each, four consecutive
+// columns of a lane in one word), rounded to 16 bytes so every slot starts
+// aligned.
 __host__ __device__ inline size_t group_slot_elems(int col_cap, int bits) {
     const size_t l = (size_t)group_lanes(bits);
-    return (size_t)col_cap * l * 2 + ((size_t)col_cap * l + 1) / 2 + 8;
+    const size_t qbytes = (((size_t)col_cap + 3) & ~(size_t)3) * l;
+    return ((size_t)col_cap * l * 2 + (qbytes + 1) / 2 + 8 + 7) & ~(size_t)7;
 }
 
 __host__ __device__ __forceinline__ unsigned umin(unsigned a, unsigned b) { return a < b ? a : b; }
@@ -74,9 +77,9 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
     const unsigned full = 0xffffffffu;
     const int t = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int16_t *Hh = A.scratch + (size_t)gw * A.slot_elems;
-    int16_t *Fv = Hh + (size_t)A.col_cap * W;
-    int8_t *Q2 = reinterpret_cast<int8_t *>(Fv + (size_t)A.col_cap * W);
+    // H (low half) and F (high half) of a lane's column in one word
+    uint32_t *HF = reinterpret_cast<uint32_t *>(A.scratch + (size_t)gw * A.slot_elems);
+    int8_t *Q2 = reinterpret_cast<int8_t *>(HF + (size_t)A.col_cap * W);
     const KernelParams &P = A.P;
     const int ngroups = (A.n + W - 1) / W;
 
@@ -170,13 +173,12 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
                 } else if (k <= maxLen2) {
                     code = 100;  // DUMMY2 (:46)
                 }
-                Q2[(size_t)k * W + l] = (int8_t)code;
+                Q2[(((size_t)(k >> 2) * W + l) << 2) + (k & 3)] = (int8_t)code;
                 int hv = 0;
                 if (k == 0) hv = h0[u];
                 else if (k == 1) hv = tt;
                 else if (k < maxLen2) { tt = E::ws(tt - e_ins); tt = tt > 0 ? tt : 0; hv = tt; }
-                Hh[(size_t)k * W + l] = (int16_t)hv;
-                Fv[(size_t)k * W + l] = 0;
+                HF[(size_t)k * W + l] = (uint16_t)hv;
             }
             // band clamp (:2882-2904 / :2183-2205): integer division, then +1.0
             const int qlenb = E::ws(len2[u] * maxsc);
@@ -211,8 +213,8 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
             exit0[u] = -1;
             max_ie[u] = 0;
         }
-        auto HH = [&](int c, int u) -> int16_t & { return Hh[(size_t)c * W + t + 32 * u]; };
-        auto FF = [&](int c, int u) -> int16_t & { return Fv[(size_t)c * W + t + 32 * u]; };
+        auto HFa = [&](int c, int u) -> uint32_t & { return HF[(size_t)c * W + t + 32 * u]; };
+        auto pack = [](int h, int f) -> uint32_t { return (uint32_t)(uint16_t)h | ((uint32_t)(uint16_t)f << 16); };
         // first column H_v[k]: h0 at k = 0, max(h0 - o_del - k e_del, 0) below
         // (wrapping), DUMMY1 at the wrapper's last row
         auto Hv = [&](int k, int u) -> int {
@@ -263,7 +265,7 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
                     for (int u = 0; u < LPT; u++) any |= head[u] > pj;
                     if (!__any_sync(full, any)) break;
                     for (int u = 0; u < LPT; u++)
-                        if (head[u] > pj || jn > tail[u]) { HH(lc, u) = 0; FF(lc, u) = 0; }
+                        if (head[u] > pj || jn > tail[u]) HFa(lc, u) = 0;
                 }
             }
             // row exit status (:3119-3129)
@@ -273,13 +275,20 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
             // DP row (:3135-3196)
             int j512 = E::ws(beg);
             int j;
+            const uint32_t *Q4 = reinterpret_cast<const uint32_t *>(Q2);
+            uint32_t qw[LPT];
             for (j = beg; j < end; j++) {
                 const int pj = j512;
                 j512 = E::ws(j512 + 1);
+                if (j == beg || (j & 3) == 0) {
+#pragma unroll
+                    for (int u = 0; u < LPT; u++) qw[u] = Q4[(size_t)(j >> 2) * W + t + 32 * u];
+                }
 #pragma unroll
                 for (int u = 0; u < LPT; u++) {
-                    const int h00 = HH(j, u), f11 = FF(j, u);
-                    const int a2 = Q2[(size_t)j * W + t + 32 * u];
+                    const uint32_t hf = HFa(j, u);
+                    const int h00 = (int16_t)(hf & 0xffffu), f11 = (int16_t)(hf >> 16);
+                    const int a2 = (int8_t)(qw[u] >> ((j & 3) * 8));
                     int sbt = s1[u] == a2 ? w_match : w_mismatch;
                     // the larger code's top bit (as unsigned): an N on either side
                     if (umax(E::us(s1[u]), E::us(a2)) > (E::MSK >> 1)) sbt = -1;
@@ -306,8 +315,7 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
                         if (cmpA) y1[u] = j512;
                         maxRS1[u] = nm;
                     }
-                    FF(j, u) = (int16_t)f21;
-                    HH(j, u) = (int16_t)hst;
+                    HFa(j, u) = pack(hst, f21);
                     h10[u] = h11;
                     if (j >= minq) {
                         const bool cq = j512 == qlen[u];
@@ -330,8 +338,7 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
             if (j < colCap) {
                 for (int u = 0; u < LPT; u++) {
                     const bool m = head[u] > j512 || j512 > tail[u];
-                    HH(j, u) = (int16_t)(m ? 0 : h10[u]);
-                    FF(j, u) = 0;
+                    HFa(j, u) = pack(m ? 0 : h10[u], 0);
                 }
             }
             // a zero row in every lane ends the group (:3206-3209)
@@ -359,7 +366,7 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
             // band narrowing (:3235-3260): columns zero in every lane
             auto all_zero = [&](int c) {
                 bool z = true;
-                for (int u = 0; u < LPT; u++) z &= (HH(c, u) | FF(c, u)) == 0;
+                for (int u = 0; u < LPT; u++) z &= HFa(c, u) == 0;
                 return __all_sync(full, z) != 0;
             };
             int lc;
@@ -375,7 +382,7 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
             {
                 bool run[LPT];
                 auto zero_at = [&](int c, int u) {
-                    return exit0[u] != 0 && (HH(c, u) | FF(c, u)) == 0;
+                    return exit0[u] != 0 && HFa(c, u) == 0;
                 };
                 for (int u = 0; u < LPT; u++) run[u] = true;
                 int l512 = E::ws(beg);
