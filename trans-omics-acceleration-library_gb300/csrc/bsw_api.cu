@@ -161,7 +161,7 @@ int launch_grouped(tal_bsw_ctx *h, const talbsw::LaunchArgs &A, int slot = 0) {
     G.P = h->kp;
     const long long ngroups = ((long long)A.n + talbsw::group_lanes(A.bits) - 1) / talbsw::group_lanes(A.bits);
     const long long slot_bytes = (long long)G.slot_elems * 2;
-    int wps = 48;  // warps per SM (tuning: TAL_BSW_GROUP_WARPS; 16 / 32 / 48 measured 97 / 108 / 121 GCUPS on C2)
+    int wps = 48;  // warps per SM, as many as fit (tuning: TAL_BSW_GROUP_WARPS; 32 / 48 measured 142 / 150 GCUPS on C2)
     if (const char *ev = getenv("TAL_BSW_GROUP_WARPS")) wps = std::min(std::max(atoi(ev), 4), 64);
     long long warps = std::min<long long>((long long)h->num_sms * wps, ngroups);
     warps = std::min<long long>(warps, std::max<long long>(4, (1LL << 30) / slot_bytes));

@@ -52,7 +52,7 @@ __host__ __device__ inline int group_lanes(int bits) { return bits == 8 ? 64 : 3
 // aligned.
 __host__ __device__ inline size_t group_slot_elems(int col_cap, int bits) {
     const size_t l = (size_t)group_lanes(bits);
-    const size_t qbytes = (((size_t)col_cap + 3) & ~(size_t)3) * l;
+    const size_t qbytes = ((((size_t)col_cap + 3) & ~(size_t)3) + 8) * l;  // + two words read ahead
     return ((size_t)col_cap * l * 2 + (qbytes + 1) / 2 + 8 + 7) & ~(size_t)7;
 }
 
@@ -272,67 +272,87 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
             for (int u = 0; u < LPT; u++)
                 if (i1 > mlen[u] || tail[u] == head[u] || head[u] > tail[u]) exit0[u] = 0;
 
-            // DP row (:3135-3196)
+            // DP row (:3135-3196), four columns at a time: their (H, F) words and
+            // query codes are loaded before the four cells are computed, so
+            // the loads overlap
             int j512 = E::ws(beg);
-            int j;
             const uint32_t *Q4 = reinterpret_cast<const uint32_t *>(Q2);
-            uint32_t qw[LPT];
-            for (j = beg; j < end; j++) {
-                const int pj = j512;
-                j512 = E::ws(j512 + 1);
-                if (j == beg || (j & 3) == 0) {
-#pragma unroll
-                    for (int u = 0; u < LPT; u++) qw[u] = Q4[(size_t)(j >> 2) * W + t + 32 * u];
+            auto cell = [&](int j, int u, uint32_t hf, int a2) {
+                const int pj = E::ws(j);
+                const int jn = E::ws(j + 1);
+                const int h00 = (int16_t)(hf & 0xffffu), f11 = (int16_t)(hf >> 16);
+                int sbt = s1[u] == a2 ? w_match : w_mismatch;
+                // the larger code's top bit (as unsigned): an N on either side
+                if (umax(E::us(s1[u]), E::us(a2)) > (E::MSK >> 1)) sbt = -1;
+                int m11 = E::ws(h00 + sbt);
+                if (h00 == 0) m11 = 0;
+                int h11 = m11 > e11[u] ? m11 : e11[u];
+                h11 = h11 > f11 ? h11 : f11;
+                int tv = E::ws(m11 - oe_ins);
+                int val = tv > 0 ? tv : 0;
+                const int ee = E::ws(e11[u] - e_ins);
+                e11[u] = val > ee ? val : ee;
+                tv = E::ws(m11 - oe_del);
+                val = tv > 0 ? tv : 0;
+                int f21 = E::ws(f11 - e_del);
+                f21 = val > f21 ? val : f21;
+                const bool cmp2 = head[u] > pj;
+                const bool mask = pj > tail[u] || cmp2;
+                const int hst = mask ? 0 : h10[u];
+                if (mask) f21 = 0;
+                const int bmax = maxRS1[u];
+                const int nm = maxRS1[u] > h11 ? maxRS1[u] : h11;
+                const bool cmpA = nm > bmax || nm == h11;
+                if (!(jn > tail[u] || cmp2)) {
+                    if (cmpA) y1[u] = jn;
+                    maxRS1[u] = nm;
                 }
+                HFa(j, u) = pack(hst, f21);
+                h10[u] = h11;
+                if (j >= minq) {
+                    const bool cq = jn == qlen[u];
+                    int max_gh = gscore[u] > h11 ? gscore[u] : h11;
+                    int t1 = gscore[u] > h11 ? max_ie[u] : i1;
+                    t1 = cq ? t1 : max_ie[u];
+                    const bool mex0 = exit0[u] < 0;
+                    t1 = mex0 ? t1 : max_ie[u];
+                    max_gh = mex0 ? max_gh : gscore[u];
+                    max_gh = cq ? max_gh : gscore[u];
+                    const bool ct = jn > tail[u];
+                    max_gh = ct ? gscore[u] : max_gh;
+                    max_ie[u] = ct ? max_ie[u] : t1;
+                    gscore[u] = max_gh;
+                }
+            };
+            // four columns per block (eight measured 147 against 150 GCUPS on C2:
+            // more registers, fewer resident warps)
+            constexpr int CB = 4;
+            for (int jb = beg; jb < end; jb += CB) {
+                const int nb = end - jb < CB ? end - jb : CB;
+                uint32_t hfb[LPT][CB], qc[LPT][CB / 4];
 #pragma unroll
                 for (int u = 0; u < LPT; u++) {
-                    const uint32_t hf = HFa(j, u);
-                    const int h00 = (int16_t)(hf & 0xffffu), f11 = (int16_t)(hf >> 16);
-                    const int a2 = (int8_t)(qw[u] >> ((j & 3) * 8));
-                    int sbt = s1[u] == a2 ? w_match : w_mismatch;
-                    // the larger code's top bit (as unsigned): an N on either side
-                    if (umax(E::us(s1[u]), E::us(a2)) > (E::MSK >> 1)) sbt = -1;
-                    int m11 = E::ws(h00 + sbt);
-                    if (h00 == 0) m11 = 0;
-                    int h11 = m11 > e11[u] ? m11 : e11[u];
-                    h11 = h11 > f11 ? h11 : f11;
-                    int tv = E::ws(m11 - oe_ins);
-                    int val = tv > 0 ? tv : 0;
-                    const int ee = E::ws(e11[u] - e_ins);
-                    e11[u] = val > ee ? val : ee;
-                    tv = E::ws(m11 - oe_del);
-                    val = tv > 0 ? tv : 0;
-                    int f21 = E::ws(f11 - e_del);
-                    f21 = val > f21 ? val : f21;
-                    const bool cmp2 = head[u] > pj;
-                    const bool mask = pj > tail[u] || cmp2;
-                    const int hst = mask ? 0 : h10[u];
-                    if (mask) f21 = 0;
-                    const int bmax = maxRS1[u];
-                    const int nm = maxRS1[u] > h11 ? maxRS1[u] : h11;
-                    const bool cmpA = nm > bmax || nm == h11;
-                    if (!(j512 > tail[u] || cmp2)) {
-                        if (cmpA) y1[u] = j512;
-                        maxRS1[u] = nm;
-                    }
-                    HFa(j, u) = pack(hst, f21);
-                    h10[u] = h11;
-                    if (j >= minq) {
-                        const bool cq = j512 == qlen[u];
-                        int max_gh = gscore[u] > h11 ? gscore[u] : h11;
-                        int t1 = gscore[u] > h11 ? max_ie[u] : i1;
-                        t1 = cq ? t1 : max_ie[u];
-                        const bool mex0 = exit0[u] < 0;
-                        t1 = mex0 ? t1 : max_ie[u];
-                        max_gh = mex0 ? max_gh : gscore[u];
-                        max_gh = cq ? max_gh : gscore[u];
-                        const bool ct = j512 > tail[u];
-                        max_gh = ct ? gscore[u] : max_gh;
-                        max_ie[u] = ct ? max_ie[u] : t1;
-                        gscore[u] = max_gh;
+#pragma unroll
+                    for (int k = 0; k < CB; k++) hfb[u][k] = k < nb ? HFa(jb + k, u) : 0u;
+                    const size_t qi = (size_t)(jb >> 2) * W + t + 32 * u;
+                    uint32_t qw[CB / 4 + 1];
+#pragma unroll
+                    for (int k = 0; k <= CB / 4; k++) qw[k] = Q4[qi + (size_t)k * W];
+#pragma unroll
+                    for (int k = 0; k < CB / 4; k++)
+                        qc[u][k] = (uint32_t)((((uint64_t)qw[k + 1] << 32) | qw[k]) >> ((jb & 3) * 8));
+                }
+#pragma unroll
+                for (int k = 0; k < CB; k++) {
+                    if (k < nb) {
+#pragma unroll
+                        for (int u = 0; u < LPT; u++)
+                            cell(jb + k, u, hfb[u][k], (int8_t)(qc[u][k >> 2] >> (8 * (k & 3))));
                     }
                 }
             }
+            const int j = beg > end ? beg : end;
+            j512 = E::ws(j);
             if (end > beg) ncells += (unsigned long long)(end - beg);
             // the row's last column (:3197-3203); j == max(beg, end) here
             if (j < colCap) {
