@@ -1,7 +1,9 @@
 """Pins the oracle (CPU restatement) to the reference: the golden fixtures
 produced by the reference itself, and -- where the reference was compiled in
-this container -- fresh seeded comparisons.  Also checks the property the GPU
-design relies on: a pair's outputs do not depend on its SIMD group."""
+this container -- fresh seeded comparisons.  Also checks the property the
+per-pair GPU kernels rely on -- a pair's outputs do not depend on its SIMD
+group -- where it holds (every workload and z-drop fixture), and the
+counter-examples where it does not (the coupled fixtures)."""
 import glob
 import os
 

@@ -4,10 +4,12 @@
 //
 // Semantics: the reference's getScores16 / getScores8 kernels
 // (src/alignment/BSW/bandedSWA.cpp:2962-3356 / :2263-2661) for a pair scored on
-// its own.  Their outputs do not depend on which other pairs share the SIMD
-// group (checked against the reference on every workload shape), so a pair is
-// the unit of work here and the per-lane head/tail bookkeeping of the vector
-// code collapses to per-pair scalars held uniformly by the pair's G lanes.
+// its own, as if alone in its SIMD group.  The reference's outputs almost
+// never depend on which other pairs share the group (equal on every workload
+// shape checked; the rare exceptions, narrow bands next to the group's, are
+// scored exactly by the grouped kernel in bsw_group.cuh), so a pair is the
+// unit of work here and the per-lane head/tail bookkeeping of the vector code
+// collapses to per-pair scalars held uniformly by the pair's G lanes.
 // Several pairs share a warp so that this per-row bookkeeping (band edges,
 // narrowing, z-drop) is paid once per warp-instruction for 32/G pairs; each
 // group takes its next pair from the work counter as soon as it finishes.

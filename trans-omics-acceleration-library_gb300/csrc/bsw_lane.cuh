@@ -2,8 +2,9 @@
 //
 // Each lane scores its own pair, row by row, exactly as the reference scores
 // one lane of its SIMD group (smithWaterman512_16 / _8, bandedSWA.cpp
-// :2962-3356 / :2263-2661, with the group reduced to that pair -- outputs do
-// not depend on the group).  There are no collectives: lanes are independent
+// :2962-3356 / :2263-2661, with the group reduced to that pair; the rare
+// outputs that depend on the group are the grouped kernel's, bsw_group.cuh).
+// There are no collectives: lanes are independent
 // and a lane that finishes a pair takes the next one from the work counter.
 // This is the GPU form of the reference's inter-task layout (one pair per SIMD
 // lane), without its shared band: every lane walks its own band.
