@@ -119,3 +119,16 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_precision_constants_match_the_header():
+    """The Python constants for the precision argument equal the header's
+    enum (TAL_BSW_AUTO / _8 / _16 and the TAL_BSW_GROUPED flag)."""
+    src = open(os.path.join(ROOT, "include", "tal_bsw.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    vals = {m.group(1): int(m.group(2), 0) for m in re.finditer(r"\b(TAL_BSW_\w+)\s*=\s*(0x[0-9a-fA-F]+|\d+)", src)}
+    assert vals["TAL_BSW_AUTO"] == tal_bsw.api.AUTO
+    assert vals["TAL_BSW_8"] == tal_bsw.api.BITS8
+    assert vals["TAL_BSW_16"] == tal_bsw.api.BITS16
+    assert vals["TAL_BSW_GROUPED"] == tal_bsw.api.GROUPED
+    assert vals["TAL_BSW_GROUPED"] & 0xff == 0

@@ -265,6 +265,30 @@ def test_grouped_device_path_and_chunked_host_call_agree():
     _assert_same(exp, host[:640], "grouped chunk 0 head")
 
 
+def test_grouped_bad_pair_in_a_later_chunk():
+    """A grouped host call of 262,144+ pairs (chunks ending on group
+    boundaries) names a bad pair in its third chunk by its index in the
+    caller's array; a device call with per-pair bands is refused."""
+    import torch
+    b = synth.generate(synth.C1_8.scaled(270_000, seed=93))
+    P = b.workload.params()
+    p = b.pairs.copy()
+    bad = 201_000
+    p["h0"][bad] = -3
+    with _bsw(P) as bsw:
+        with pytest.raises(tal_bsw.TalBswError) as ei:
+            bsw._scores(p, b.ref, b.qer, b.n, 100, 8 | GROUPED)
+        assert ei.value.status == tal_bsw.api.TAL_EDOMAIN and ei.value.bad_pair == bad
+        dp = torch.from_numpy(b.pairs[:64].view(np.uint8).reshape(-1).copy()).cuda()
+        dr = torch.from_numpy(b.ref).cuda()
+        dq = torch.from_numpy(b.qer).cuda()
+        dw = torch.full((64,), 100, dtype=torch.int32, device="cuda")
+        with pytest.raises(tal_bsw.TalBswError) as ei:
+            bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(), 64,
+                              100, bits=8 | GROUPED, d_w=dw.data_ptr())
+        assert ei.value.status == tal_bsw.api.TAL_EINVAL
+
+
 def test_grouped_refusals():
     b = synth.generate(synth.C2.scaled(64, seed=5))
     P = b.workload.params()
