@@ -302,3 +302,27 @@ def test_grouped_refusals():
         with pytest.raises(tal_bsw.TalBswError) as ei:
             bsw._scores(p, b.ref, b.qer, b.n, 100, 16 | GROUPED)
         assert ei.value.status == tal_bsw.api.TAL_EDOMAIN and ei.value.bad_pair == 40
+
+
+@pytest.mark.parametrize("wl,n", [(synth.C1, 100_000), (synth.C1_8, 100_000), (synth.C3, 2_000_000),
+                                  (synth.C4, 4_000)])
+def test_per_pair_equals_grouped_on_workloads(wl, n):
+    """At workload sizes no oracle finishes quickly: the per-pair kernels and
+    the grouped kernel (the reference's own grouping) give the same outputs
+    on every pair, per (band, precision) call as the reference's caller
+    would split a mixed batch."""
+    b = synth.generate(wl, n)
+    P = wl.params()
+    warr = b.w if wl.w_choices else np.full(b.n, wl.w, np.int32)
+    is8 = oracle.eligible8(b.pairs, warr, P) if wl.bits == 0 else np.full(b.n, wl.bits == 8)
+    with _bsw(P) as bsw:
+        for wv in np.unique(warr):
+            for bits in (8, 16):
+                sel = np.nonzero((warr == wv) & (is8 == (bits == 8)))[0]
+                if not sel.size:
+                    continue
+                a = b.pairs[sel].copy()
+                g = b.pairs[sel].copy()
+                bsw._scores(a, b.ref, b.qer, a.shape[0], int(wv), bits)
+                bsw._scores(g, b.ref, b.qer, g.shape[0], int(wv), bits | GROUPED)
+                _assert_same(g, a, f"{wl.name} w={wv} bits={bits}: per pair vs grouped")
