@@ -282,8 +282,9 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
                 const int jn = E::ws(j + 1);
                 const int h00 = (int16_t)(hf & 0xffffu), f11 = (int16_t)(hf >> 16);
                 int sbt = s1[u] == a2 ? w_match : w_mismatch;
-                // the larger code's top bit (as unsigned): an N on either side
-                if (umax(E::us(s1[u]), E::us(a2)) > (E::MSK >> 1)) sbt = -1;
+                // the larger code's top bit (as unsigned): an N on either side;
+                // codes are held sign-extended, so that is either being negative
+                if ((s1[u] | a2) < 0) sbt = -1;
                 int m11 = E::ws(h00 + sbt);
                 if (h00 == 0) m11 = 0;
                 int h11 = m11 > e11[u] ? m11 : e11[u];
@@ -309,19 +310,13 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
                 }
                 HFa(j, u) = pack(hst, f21);
                 h10[u] = h11;
-                if (j >= minq) {
-                    const bool cq = jn == qlen[u];
-                    int max_gh = gscore[u] > h11 ? gscore[u] : h11;
-                    int t1 = gscore[u] > h11 ? max_ie[u] : i1;
-                    t1 = cq ? t1 : max_ie[u];
-                    const bool mex0 = exit0[u] < 0;
-                    t1 = mex0 ? t1 : max_ie[u];
-                    max_gh = mex0 ? max_gh : gscore[u];
-                    max_gh = cq ? max_gh : gscore[u];
-                    const bool ct = jn > tail[u];
-                    max_gh = ct ? gscore[u] : max_gh;
-                    max_ie[u] = ct ? max_ie[u] : t1;
-                    gscore[u] = max_gh;
+                // end-to-end score (:3178-3195): the blends there change gscore
+                // and max_ie only in the query's last column (j + 1 == qlen,
+                // which implies j >= minq), in a live lane, left of the tail,
+                // and only where h11 is not below the current gscore
+                if (j >= minq && jn == qlen[u] && exit0[u] < 0 && !(jn > tail[u]) && !(gscore[u] > h11)) {
+                    gscore[u] = h11;
+                    max_ie[u] = i1;
                 }
             };
             // four columns per block (eight measured 147 against 150 GCUPS on C2:
