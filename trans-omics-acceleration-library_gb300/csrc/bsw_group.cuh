@@ -226,6 +226,8 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
             return 99;  // DUMMY1 (:45)
         };
         unsigned long long ncells = 0;
+        int tnext[LPT];  // the next row's target base
+        for (int u = 0; u < LPT; u++) tnext[u] = len1[u] > 0 ? A.ref[idr[u] - A.ref_lo] : 0;
         int beg = 0, end = ncol, nbeg = 0, nend = ncol;
         for (int i = 0; i < nrow; i++) {
             const int i1 = E::ws(i + 1);
@@ -239,7 +241,8 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
                 e11[u] = 0; maxRS1[u] = 0; y1[u] = 0;
                 h10[u] = beg == 0 ? Hv(i + 1, u) : 0;
                 if (i < len1[u]) {
-                    const int b = A.ref[idr[u] - A.ref_lo + i];
+                    const int b = tnext[u];  // loaded a row ahead
+                    if (i + 1 < len1[u]) tnext[u] = A.ref[idr[u] - A.ref_lo + i + 1];
                     s1[u] = b == 4 ? -1 : E::ws(b);
                     if (b > 4) {
                         atomicOr(A.err_flags, ERR_BASE);
@@ -320,30 +323,39 @@ __global__ void __launch_bounds__(128) bsw_group_kernel(GroupArgs A) {
                 }
             };
             // four columns per block (eight measured 147 against 150 GCUPS on C2:
-            // more registers, fewer resident warps)
+            // more registers, fewer resident warps); the next block's words
+            // are loaded before this block is computed (blocks never share a
+            // column, so the loads see this row's inputs)
             constexpr int CB = 4;
-            for (int jb = beg; jb < end; jb += CB) {
+            uint32_t hfb[LPT][CB], qc[LPT];
+            auto load_block = [&](int jb, uint32_t (&hv)[LPT][CB], uint32_t (&qv)[LPT]) {
                 const int nb = end - jb < CB ? end - jb : CB;
-                uint32_t hfb[LPT][CB], qc[LPT][CB / 4];
 #pragma unroll
                 for (int u = 0; u < LPT; u++) {
 #pragma unroll
-                    for (int k = 0; k < CB; k++) hfb[u][k] = k < nb ? HFa(jb + k, u) : 0u;
+                    for (int k = 0; k < CB; k++) hv[u][k] = k < nb ? HFa(jb + k, u) : 0u;
                     const size_t qi = (size_t)(jb >> 2) * W + t + 32 * u;
-                    uint32_t qw[CB / 4 + 1];
-#pragma unroll
-                    for (int k = 0; k <= CB / 4; k++) qw[k] = Q4[qi + (size_t)k * W];
-#pragma unroll
-                    for (int k = 0; k < CB / 4; k++)
-                        qc[u][k] = (uint32_t)((((uint64_t)qw[k + 1] << 32) | qw[k]) >> ((jb & 3) * 8));
+                    const uint64_t q2 = (uint64_t)Q4[qi] | ((uint64_t)Q4[qi + W] << 32);
+                    qv[u] = (uint32_t)(q2 >> ((jb & 3) * 8));
                 }
+            };
+            if (beg < end) load_block(beg, hfb, qc);
+            for (int jb = beg; jb < end; jb += CB) {
+                const int nb = end - jb < CB ? end - jb : CB;
+                uint32_t hfn[LPT][CB] = {}, qn[LPT] = {};
+                if (jb + CB < end) load_block(jb + CB, hfn, qn);
 #pragma unroll
                 for (int k = 0; k < CB; k++) {
                     if (k < nb) {
 #pragma unroll
-                        for (int u = 0; u < LPT; u++)
-                            cell(jb + k, u, hfb[u][k], (int8_t)(qc[u][k >> 2] >> (8 * (k & 3))));
+                        for (int u = 0; u < LPT; u++) cell(jb + k, u, hfb[u][k], (int8_t)(qc[u] >> (8 * k)));
                     }
+                }
+#pragma unroll
+                for (int u = 0; u < LPT; u++) {
+                    qc[u] = qn[u];
+#pragma unroll
+                    for (int k = 0; k < CB; k++) hfb[u][k] = hfn[u][k];
                 }
             }
             const int j = beg > end ? beg : end;
