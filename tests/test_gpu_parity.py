@@ -172,8 +172,9 @@ def test_host_call_in_chunks():
 def test_long_queries_near_the_16_bit_limit():
     """Queries of 20,000-32,700 bases: narrow bands in rings (lane kernel),
     a band of 8,000 in a 16,384-column ring (G lanes per pair), a band of
-    10,000 in whole rows of 22,000 columns; a query of 30,000 with a band of
-    20,000 needs more shared memory than a block has: TAL_EDOMAIN."""
+    10,000 in whole rows of 22,000 columns, and each in the grouped kernel; a
+    query of 30,000 with a band of 20,000 needs more shared memory than a
+    block has for the per-pair kernels: TAL_EDOMAIN."""
     from _cases import DEFAULT, pack
     rng = np.random.default_rng(77)
 
@@ -190,6 +191,9 @@ def test_long_queries_near_the_16_bit_limit():
         exp = oracle.vector(p, r, q, w, DEFAULT, bits=16)
         got = _gpu(p, r, q, w, DEFAULT, 16)
         _assert_same(exp, got, f"long queries, w={w}")
+        # the grouped kernel keeps its rows in global scratch: same outputs
+        got = _gpu(p, r, q, w, DEFAULT, 16 | tal_bsw.api.GROUPED)
+        _assert_same(exp, got, f"long queries, w={w}, grouped")
     refs, qers = zip(*[pair(30000, 0)])
     p, r, q = pack(list(refs), list(qers), [50])
     with _bsw(DEFAULT) as bsw:
