@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only.  Nothing in the product library links or
 // calls this file; tests/, __graft_entry__.smoke() and bench.py's CPU legs load
-// it as the checker / CPU baseline.
+// it as the test oracle / CPU baseline.
 //
 // A CPU restatement, written from the reference's algorithm, of TAL's banded
 // Smith-Waterman seed extension (src/alignment/BSW/bandedSWA.cpp):
