@@ -169,3 +169,27 @@ def coupled_cases():
         qs = [qer[int(x["idq"]):int(x["idq"]) + int(x["len2"])] for x in sub]
         cp, cr, cq = pack(ts, qs, sub["h0"])
         yield name, cp, cr, cq, w, bits
+
+
+def wrapping_cases():
+    """8-bit pair sets with gap opens whose int8 sums wrap (o + e = 130 > 127):
+    outside the per-pair kernels' exact range (TAL_EDOMAIN there), scored by
+    the grouped kernel, whose values wrap as the reference's do; a third to a
+    half of these pairs get other outputs in their group than alone.  70
+    pairs: one full group of 64 and a partial one (the padding lanes read the
+    query bytes at offset 0).  Yields (name, pairs, ref, qer, w, P)."""
+    rng = np.random.default_rng(3)
+    P = dict(o_del=120, e_del=10, o_ins=120, e_ins=10, zdrop=100, end_bonus=5, a=1, b=4)
+    refs, qers, h0s = [], [], []
+    for _ in range(70):
+        L = int(rng.integers(5, 120))
+        q = rng.integers(0, 4, L).astype(np.uint8)
+        r = q.copy()
+        m = rng.random(L) < 0.1
+        r[m] = (r[m] + 1) % 4
+        refs.append(np.concatenate([r, rng.integers(0, 4, int(rng.integers(0, 8))).astype(np.uint8)]))
+        qers.append(q)
+        h0s.append(int(rng.integers(0, 20)))
+    p, ref, qer = pack(refs, qers, h0s)
+    for w in (5, 126):
+        yield f"wrap8_gap_open_130_band_{w}", p, ref, qer, w, P

@@ -18,7 +18,7 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "trans-omics-acceleration-library_gb300
                 os.path.dirname(HERE)]
 
 import oracle  # noqa: E402
-from _cases import DEFAULT, coupled_cases, edge_cases, workload_slices  # noqa: E402
+from _cases import DEFAULT, coupled_cases, edge_cases, workload_slices, wrapping_cases  # noqa: E402
 
 KEYS = ["o_del", "e_del", "o_ins", "e_ins", "zdrop", "end_bonus", "a", "b"]
 
@@ -61,6 +61,8 @@ def main():
             save(f"edge{bits}_{name}", p, r, q, w, P, bits)
     for name, p, r, q, w, bits in coupled_cases():
         save(name, p, r, q, w, DEFAULT, bits)
+    for name, p, r, q, w, P in wrapping_cases():
+        save(name, p, r, q, w, P, 8)
 
 
 if __name__ == "__main__":

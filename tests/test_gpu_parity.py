@@ -74,7 +74,7 @@ def test_edge_cases(bits):
 
 def test_golden_fixtures():
     files = [f for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
-             if not os.path.basename(f).startswith("coupled")]
+             if not os.path.basename(f).startswith(("coupled", "wrap8"))]
     assert files, "no golden fixtures"
     for f in files:
         d = np.load(f)
@@ -267,6 +267,18 @@ def test_grouped_device_path_and_chunked_host_call_agree():
     _assert_same(host, dev, "grouped host vs device")
     exp = oracle.vector(b.pairs[:640], b.ref, b.qer, 100, P, bits=8)
     _assert_same(exp, host[:640], "grouped chunk 0 head")
+
+
+def test_wrapping_fixtures_grouped_only():
+    """Gap opens whose int8 sums wrap: the per-pair 8-bit kernels refuse the
+    pairs (outside their exact range), the grouped kernel gives the
+    reference's outputs (checked by test_grouped_matches_golden)."""
+    for f in sorted(glob.glob(os.path.join(GOLDEN, "wrap8*.npz"))):
+        d = np.load(f)
+        P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+        with pytest.raises(tal_bsw.TalBswError) as ei:
+            _gpu(d["inputs"], d["ref"], d["qer"], d["w"], P, 8)
+        assert ei.value.status == tal_bsw.api.TAL_EDOMAIN
 
 
 def test_grouped_bad_pair_in_a_later_chunk():
