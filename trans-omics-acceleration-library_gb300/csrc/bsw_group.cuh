@@ -57,7 +57,6 @@ __host__ __device__ inline size_t group_slot_elems(int col_cap, int bits) {
 }
 
 __host__ __device__ __forceinline__ unsigned umin(unsigned a, unsigned b) { return a < b ? a : b; }
-__host__ __device__ __forceinline__ unsigned umax(unsigned a, unsigned b) { return a > b ? a : b; }
 
 // Element-width helpers: S = 16 or 8 bits; values are held sign-extended.
 template <int SB>
