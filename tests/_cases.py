@@ -177,7 +177,9 @@ def wrapping_cases():
     the grouped kernel, whose values wrap as the reference's do; a third to a
     half of these pairs get other outputs in their group than alone.  70
     pairs: one full group of 64 and a partial one (the padding lanes read the
-    query bytes at offset 0).  Yields (name, pairs, ref, qer, w, P)."""
+    query bytes at offset 0).  Then 16-bit pairs whose h0 is within 270 of the
+    int16 limit, so their DP values wrap.  Yields (name, pairs, ref, qer, w,
+    P, bits)."""
     rng = np.random.default_rng(3)
     P = dict(o_del=120, e_del=10, o_ins=120, e_ins=10, zdrop=100, end_bonus=5, a=1, b=4)
     refs, qers, h0s = [], [], []
@@ -192,4 +194,17 @@ def wrapping_cases():
         h0s.append(int(rng.integers(0, 20)))
     p, ref, qer = pack(refs, qers, h0s)
     for w in (5, 126):
-        yield f"wrap8_gap_open_130_band_{w}", p, ref, qer, w, P
+        yield f"wrap8_gap_open_130_band_{w}", p, ref, qer, w, P, 8
+    # 16-bit: h0 within 270 of the int16 limit, so the DP values wrap
+    refs, qers, h0s = [], [], []
+    for _ in range(40):
+        L = int(rng.integers(50, 300))
+        q = rng.integers(0, 4, L).astype(np.uint8)
+        r = q.copy()
+        m = rng.random(L) < 0.05
+        r[m] = (r[m] + 1) % 4
+        refs.append(np.concatenate([r, rng.integers(0, 4, int(rng.integers(0, 30))).astype(np.uint8)]))
+        qers.append(q)
+        h0s.append(int(rng.integers(32500, 32768)))
+    p, ref, qer = pack(refs, qers, h0s)
+    yield "wrap16_h0_near_limit_band_100", p, ref, qer, 100, DEFAULT, 16

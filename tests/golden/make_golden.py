@@ -61,8 +61,8 @@ def main():
             save(f"edge{bits}_{name}", p, r, q, w, P, bits)
     for name, p, r, q, w, bits in coupled_cases():
         save(name, p, r, q, w, DEFAULT, bits)
-    for name, p, r, q, w, P in wrapping_cases():
-        save(name, p, r, q, w, P, 8)
+    for name, p, r, q, w, P, bits in wrapping_cases():
+        save(name, p, r, q, w, P, bits)
 
 
 if __name__ == "__main__":

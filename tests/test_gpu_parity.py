@@ -74,7 +74,7 @@ def test_edge_cases(bits):
 
 def test_golden_fixtures():
     files = [f for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
-             if not os.path.basename(f).startswith(("coupled", "wrap8"))]
+             if not os.path.basename(f).startswith(("coupled", "wrap"))]
     assert files, "no golden fixtures"
     for f in files:
         d = np.load(f)
@@ -270,14 +270,17 @@ def test_grouped_device_path_and_chunked_host_call_agree():
 
 
 def test_wrapping_fixtures_grouped_only():
-    """Gap opens whose int8 sums wrap: the per-pair 8-bit kernels refuse the
-    pairs (outside their exact range), the grouped kernel gives the
-    reference's outputs (checked by test_grouped_matches_golden)."""
-    for f in sorted(glob.glob(os.path.join(GOLDEN, "wrap8*.npz"))):
+    """Gap opens whose int8 sums wrap, and 16-bit scores that wrap past the
+    int16 limit: the per-pair kernels refuse the pairs (outside their exact
+    range), the grouped kernel gives the reference's outputs (checked by
+    test_grouped_matches_golden)."""
+    files = sorted(glob.glob(os.path.join(GOLDEN, "wrap*.npz")))
+    assert len(files) >= 3
+    for f in files:
         d = np.load(f)
         P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
         with pytest.raises(tal_bsw.TalBswError) as ei:
-            _gpu(d["inputs"], d["ref"], d["qer"], d["w"], P, 8)
+            _gpu(d["inputs"], d["ref"], d["qer"], d["w"], P, int(d["bits"]))
         assert ei.value.status == tal_bsw.api.TAL_EDOMAIN
 
 

@@ -16,9 +16,9 @@ ALL_FILES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
 # fixtures whose reference outputs depend on the SIMD grouping: the per-pair
 # kernels are checked on them against pair-at-a-time scoring instead
 COUPLED = [f for f in ALL_FILES if os.path.basename(f).startswith("coupled")]
-# fixtures outside the per-pair kernels' exact range (int8 gap sums that wrap):
-# grouped kernel only
-WRAPPING = [f for f in ALL_FILES if os.path.basename(f).startswith("wrap8")]
+# fixtures outside the per-pair kernels' exact range (int8 gap sums or int16
+# scores that wrap): grouped kernel only
+WRAPPING = [f for f in ALL_FILES if os.path.basename(f).startswith("wrap")]
 FILES = [f for f in ALL_FILES if f not in COUPLED and f not in WRAPPING]
 CONFIGS = [(1, 4), (4, 4), (8, 4), (8, 2), (16, 4), (32, 4), (32, 2), (4, 2), (16, 2)]
 
