@@ -55,6 +55,10 @@ def _oracle():
         lib.oracle_sw.restype = ctypes.c_int
         lib.oracle_sw.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                   ctypes.c_int64, ctypes.c_int]
+        lib.oracle_bsw_detect.restype = ctypes.c_int
+        lib.oracle_bsw_detect.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_int32, ctypes.c_void_p, ctypes.c_int]
         lib.oracle_bsw_scalar.restype = ctypes.c_int
         lib.oracle_bsw_scalar.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
@@ -84,6 +88,22 @@ def vector(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w: int,
     if rc != 0:
         raise ValueError("oracle_bsw_vector rejected its arguments")
     return out
+
+
+def detect(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w: int,
+           params: Dict[str, int], bits: int = 16, nthreads: int = 1):
+    """The library's group-coupling detector restated: every pair scored alone
+    (the per-pair kernels' outputs) and a flag per pair, non-zero where its
+    outputs may depend on the other pairs of its SIMD group.  Returns
+    (scored copy, flags)."""
+    out = np.ascontiguousarray(pairs).copy()
+    flags = np.zeros(out.shape[0], np.int32)
+    pv = _params(params)
+    rc = _oracle().oracle_bsw_detect(_ptr(pv), bits, _ptr(out), out.shape[0], _ptr(ref),
+                                     _ptr(qer), int(w), _ptr(flags), nthreads)
+    if rc != 0:
+        raise ValueError("oracle_bsw_detect rejected its arguments")
+    return out, flags
 
 
 def scalar(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w: int,

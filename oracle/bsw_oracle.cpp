@@ -556,6 +556,281 @@ int scalar_pair(const Params &P, const int8_t *mat, int qlen, const uint8_t *que
     return max;
 }
 
+// The library's group-coupling detector, restated for testing (the GPU
+// kernels compute the same flag, csrc/bsw_couple.cuh).  Scores one pair as
+// if alone in its SIMD group -- the oracle's W = 1 path -- and returns a
+// non-zero flag unless its outputs provably equal its outputs in ANY group of
+// the reference (bandedSWA.cpp:3053-3316, :2355-2621).  A group influences a
+// lane only through values it shares: the band [beg, end) of each row, the
+// trimming pass, the ranges of the head / tail re-derivation scans and the
+// width of its row-0 initialisation (the longest query).  For each, the check
+// below bounds the group's value (beg >= i - w, end <= i + w + 1, scans from
+// any nbeg' <= nbeg to any nend' <= end + 2, width up to the element limit)
+// and verifies that every value in the bound leaves the lane's stored row
+// and outputs unchanged; the head and tail the group could hold instead of
+// the lane's own are carried as intervals [hlo, hhi], [tlo, thi].
+template <typename S>
+int detect_pair(const Params &P, Pair *p, const uint8_t *ref, const uint8_t *qer, int32_t w_call) {
+    typedef Lane<S> L; typedef typename L::U U;
+    const bool is16 = sizeof(S) == 2;
+    const int CMAX = is16 ? 32767 : 127;
+    const S w_match = L::wrap((int8_t)P.a), w_mismatch = L::wrap((int8_t)(P.b * -1)), w_ambig = L::wrap(-1);
+    const S e_del = L::wrap(P.e_del), oe_del = L::wrap(P.o_del + P.e_del);
+    const S e_ins = L::wrap(P.e_ins), oe_ins = L::wrap(P.o_ins + P.e_ins), o_del = L::wrap(P.o_del);
+    const S zdropv = L::wrap(P.zdrop);
+    S maxsc = 0;
+    if (maxsc < (int8_t)P.a) maxsc = L::wrap((int8_t)P.a);
+    if (maxsc < (int8_t)(P.b * -1)) maxsc = L::wrap((int8_t)(P.b * -1));
+    if (maxsc < -1) maxsc = L::wrap(-1);
+    const int len1 = p->len1, len2 = p->len2;
+    const int nrow = len1, ncol = len2;
+    std::vector<S> s1(len1 + 3), s2(len2 + 3), Hh(len2 + 3), Hv(len1 + 3), F(len2 + 3);
+    const S ambv = L::ones();
+    const S h0 = L::wrap((U)p->h0);
+    for (int k = 0; k < len1; k++) { uint8_t b = ref[p->idr + k]; s1[k] = b == AMBIG ? ambv : L::wrap(b); }
+    Hv[len1] = DUMMY1; s1[len1] = DUMMY1;
+    Hv[0] = h0;
+    { S t = L::wrap(h0 - o_del); for (int k = 1; k < len1; k++) { t = L::wrap(t - e_del); Hv[k] = t > 0 ? t : 0; } }
+    for (int k = 0; k < len2; k++) { uint8_t b = qer[p->idq + k]; s2[k] = b == AMBIG ? ambv : L::wrap(b); }
+    s2[len2] = DUMMY2; Hh[len2] = 0;
+    Hh[0] = h0;
+    const int v1 = (h0 > oe_ins) ? (int)L::wrap(h0 - oe_ins) : 0;
+    { S t = (S)v1; Hh[1] = t;
+      for (int k = 2; k < len2; k++) { S dd = L::wrap(t - e_ins); t = dd > 0 ? dd : 0; Hh[k] = t; } }
+    // row-0 values are positive exactly at columns 1 <= k < K0 (and at 0 when h0 > 0)
+    const int K0 = v1 > 0 ? (v1 - 1) / (int)e_ins + 2 : 1;
+    auto initA_pos = [&](int c) { return c == 0 ? h0 > 0 : c == 1 ? v1 > 0 : (c < len2 && c < K0); };
+    int32_t bsize = w_call; S myband;
+    {
+        const S eb_ins = L::wrap(P.end_bonus - P.o_ins), eb_del = L::wrap(P.end_bonus - P.o_del);
+        S qlenb = L::wrap((U)(len2 * maxsc));
+        U temp = (U)L::wrap(qlenb + eb_ins); double val = temp / P.e_ins + 1.0; int mi = (int)val; mi = mi > 1 ? mi : 1;
+        myband = L::wrap((U)(bsize > mi ? mi : bsize));
+        temp = (U)L::wrap(qlenb + eb_del); val = temp / P.e_del + 1.0; mi = (int)val; mi = mi > 1 ? mi : 1;
+        int mb = (int)(U)myband; myband = L::wrap((U)(mb > mi ? mi : mb));
+        if (bsize < (int)(U)myband) bsize = (int)(U)myband;
+    }
+    const int32_t w = bsize;
+    const S tlen = L::wrap((U)len1), qlen = L::wrap((U)len2);
+    S head = 0, tail = qlen;
+    int hlo = 0, hhi = 0, tlo = (int)qlen, thi = (int)qlen;
+    const S mlen = L::wrap(std::min<U>((U)L::wrap(qlen + myband), (U)tlen));
+    S maxScore = Hv[0], x = 0, y = 0, gscore = -1, max_off = 0, max_ie = 0; bool ex = true;
+    const int minq = len2 - 1;
+    int flag = 0;
+    int beg = 0, end = ncol, nbeg = 0, nend = ncol;
+    int frozenTo = 0, fzMax = -1, fzMin = 1 << 30;
+    int maxEnd = -1;             // furthest column written so far
+    bool reachedLen2 = false;
+    int Fv = 0;
+    auto nzA = [&](int c) -> bool { return c >= 0 && c <= len2 && ((Hh[c] | F[c]) != 0); };
+    // first column in (a, b] that may be nonzero right of everything written (a >= end)
+    auto firstRightNZ = [&](int a, int b) -> int {
+        // A's own columns: written ones in (end, maxEnd] are zero; beyond: row-0 values
+        int c0 = std::max(a, maxEnd) + 1;
+        if (c0 <= b && c0 < len2 && initA_pos(c0)) return c0;
+        if (c0 <= b && c0 <= 1 && initA_pos(1) && 1 < len2 && 1 <= b) return 1;
+        // column len2 in the group's view
+        if (len2 > a && len2 <= b) {
+            bool nz = (len2 <= maxEnd ? nzA(len2) : false) || Fv > 0 || (!reachedLen2 && len2 >= 2 && len2 < K0) || (len2 == 1 && !reachedLen2 && v1 > 0);
+            if (nz) return len2;
+        }
+        int c1 = std::max(a, len2) + 1;
+        if (c1 <= b && c1 < CMAX && c1 < K0) return c1;
+        return -1;
+    };
+    auto score = [&](int i, int j) -> S {
+        const S a1 = s1[i], a2 = s2[j];
+        S sbt = (a1 == a2) ? w_match : w_mismatch;
+        if (L::topbit((S)std::max<U>((U)a1, (U)a2))) sbt = w_ambig;
+        return sbt;
+    };
+    auto FL = [&](int b, int) { flag |= b; };
+    for (int i = 0; i < nrow; i++) {
+        const S i1 = L::wrap(i + 1);
+        S e11 = 0, maxRS1 = 0, y1 = 0;
+        beg = nbeg; end = nend;
+        if (beg < i - w) beg = i - w;
+        if (end > i + w + 1) end = i + w + 1;
+        if (end > ncol) end = ncol;
+        for (int c = frozenTo; c < beg; c++) if (nzA(c)) { fzMax = std::max(fzMax, c); fzMin = std::min(fzMin, c); }
+        frozenTo = std::max(frozenTo, beg);
+        S h10 = (beg == 0) ? Hv[i + 1] : (S)0;
+        const S h10init = h10;
+        const S ph = head, pt = tail;
+        {
+            S c = L::wrap(i - myband); head = head > c ? head : c;
+            hlo = std::max(hlo, (int)c); hhi = std::max(hhi, (int)c);
+            U c2 = (U)L::wrap(i1 + myband);
+            U t = std::min<U>((U)tail, c2); t = std::min<U>(t, (U)qlen); tail = (S)t;
+            tlo = (int)(S)std::min<U>(std::min<U>((U)(S)tlo, c2), (U)qlen);
+            thi = (int)(S)std::min<U>(std::min<U>((U)(S)thi, c2), (U)qlen);
+        }
+        const bool changed = head != ph || tail != pt;
+        const bool wasActive = ex;
+        if (i1 > mlen || tail == head || head > tail) ex = false;
+        const bool active = wasActive && ex;
+        const bool uncH = hlo != hhi;
+        const int lo = std::max(0, i - w);
+        const int Emax = std::min(i + w + 1, CMAX);
+        if (wasActive && !(i1 > mlen) && tlo <= hhi && thi > hlo) FL(1 << 12, i);
+        bool unmaskedRight = false;
+        if (active) {
+            if (tlo != thi) FL(1 << 14, i);            // tail uncertainty: flagged
+            if (uncH && hhi > end) FL(1 << 13, i);
+            // old values on [beg, min(end, max(head, hhi))): the masked-left loop (and [head, hhi))
+            if (!changed || uncH) {
+                for (int c = beg; c < std::min(end, std::max((int)head, hhi)); c++) if (nzA(c)) { FL(1, i); break; }
+            }
+            if (uncH && beg >= hlo && beg < hhi && h10init != 0) FL(1 << 13, i);
+            if (beg > lo) {
+                const bool anyNZ = fzMax >= lo;
+                if (!anyNZ) {
+                    if (lo == 0 && hlo <= 0 && Hv[i + 1] != 0) FL(2, i);
+                } else if (hlo < beg && tail >= std::max(lo, hlo)) FL(2, i);
+                else {
+                    for (int j = lo; j < beg; j++) {
+                        if (Hh[j] != 0) {
+                            int M = (int)Hh[j] + (int)score(i, j);
+                            if (M - (int)oe_ins - (beg - 1 - j) * (int)e_ins > 0) { FL(4, i); break; }
+                        }
+                    }
+                    if (hlo <= beg && beg <= thi && nzA(beg - 1)) FL(8, i);
+                }
+            }
+            if (end < Emax) {
+                if (end < thi) unmaskedRight = true;
+                // stale row-0 values right of everything written, left of Emax
+                const int a = std::max(end, tlo);
+                int c0 = std::max(a, maxEnd) + 1;
+                if (c0 <= std::min(Emax, len2 - 1) && initA_pos(c0)) FL(32, i);
+            }
+        }
+        if (changed) {
+            for (int lc = beg; lc < end; lc++) {
+                const S pj = L::wrap(lc), jn = L::wrap(lc + 1);
+                if (!(head > pj)) break;
+                if (head > pj || jn > tail) { Hh[lc] = 0; F[lc] = 0; }
+            }
+        }
+        S j512 = L::wrap(beg);
+        int j;
+        S f21_tail = 0; bool tail_in = false;
+        S oldHhEnd = (end <= len2) ? Hh[end] : 0, oldFEnd = (end <= len2) ? F[end] : 0;
+        for (j = beg; j < end; j++) {
+            const S pj = j512; j512 = L::wrap(j512 + 1);
+            const S h00 = Hh[j], f11 = F[j];
+            S sbt = score(i, j);
+            S m11 = L::wrap(h00 + sbt); if (h00 == 0) m11 = 0;
+            S h11 = m11 > e11 ? m11 : e11; h11 = h11 > f11 ? h11 : f11;
+            S t = L::wrap(m11 - oe_ins); S val = t > 0 ? t : 0; S e = L::wrap(e11 - e_ins); e11 = val > e ? val : e;
+            t = L::wrap(m11 - oe_del); val = t > 0 ? t : 0; S f21 = L::wrap(f11 - e_del); f21 = val > f21 ? val : f21;
+            if (j == tail) { f21_tail = f21; tail_in = true; }
+            const bool cmp2 = head > pj; const bool mask = (pj > tail) || cmp2;
+            S hst = mask ? (S)0 : h10; if (mask) f21 = 0;
+            const S bmax = maxRS1; S nm = maxRS1 > h11 ? maxRS1 : h11;
+            const bool cmpA = (nm > bmax) || (nm == h11); const bool cmp1b = (j512 > tail) || cmp2;
+            if (!cmp1b) { if (cmpA) y1 = j512; maxRS1 = nm; }
+            F[j] = f21; Hh[j] = hst; h10 = h11;
+            if (j >= minq) {
+                const bool cq = j512 == qlen; S max_gh = gscore > h11 ? gscore : h11; const bool cgh = gscore > h11;
+                S t1 = cgh ? max_ie : i1; t1 = cq ? t1 : max_ie; t1 = ex ? t1 : max_ie;
+                max_gh = ex ? max_gh : gscore; max_gh = cq ? max_gh : gscore;
+                const bool ct = j512 > tail; max_gh = ct ? gscore : max_gh; max_ie = ct ? max_ie : t1; gscore = max_gh;
+            }
+        }
+        if (active) {
+            if (unmaskedRight) {
+                bool z = e11 == 0 && oldHhEnd == 0 && oldFEnd == 0;
+                int c0 = std::max(end, maxEnd) + 1;
+                if (z && c0 <= std::min(Emax, len2 - 1) && initA_pos(c0)) z = false;
+                if (len2 - 1 >= end && len2 - 1 < Emax && thi >= len2 && gscore <= 0) z = false;
+                if (!z) FL(16, i);
+            }
+            if (tail_in && f21_tail != 0 && (int)tail < Emax) FL(64, i);
+            if (end < Emax && end == tail && head <= end && end < len2) {
+                S sbt = score(i, end);
+                S m11 = L::wrap(oldHhEnd + sbt); if (oldHhEnd == 0) m11 = 0;
+                S t = L::wrap(m11 - oe_del); S val = t > 0 ? t : 0; S f21 = L::wrap(oldFEnd - e_del); f21 = val > f21 ? val : f21;
+                if (f21 != 0) FL(128, i);
+            }
+        }
+        {   const bool m = (head > j512) || (j512 > tail);
+            if (j <= len2) { Hh[j] = m ? (S)0 : h10; F[j] = 0; } }
+        maxEnd = std::max(maxEnd, j);
+        if (j == len2) {
+            reachedLen2 = true;
+            const S hv = Hh[len2];
+            const int sc = (s1[i] == ambv) ? -1 : (int)w_mismatch;
+            int M = hv ? (int)hv + sc : 0;
+            int nf = std::max(Fv - (int)e_del, std::max(M - (int)oe_del, 0));
+            Fv = (len2 > tail || head > len2) ? 0 : nf;
+        }
+        if (maxRS1 == 0) { ex = false; break; }
+        {
+            const S bmaxScore = maxScore; const S sc2 = maxScore > maxRS1 ? maxScore : maxRS1;
+            if (ex) maxScore = sc2;
+            if (maxScore > bmaxScore) { y = y1; x = i1; S ind = L::wrap(y1 - i1); ind = (ind < 0) ? L::wrap(-ind) : ind; max_off = max_off > ind ? max_off : ind; }
+            const S tmpi = L::wrap(i1 - x), tmpj = L::wrap(y1 - y); const bool cz = tmpi > tmpj;
+            const S sc = L::wrap(maxScore - maxRS1); const S d = cz ? L::wrap(tmpi - tmpj) : L::wrap(tmpj - tmpi);
+            if (L::wrap(sc - d) > zdropv) ex = false;
+        }
+        int lc;
+        for (lc = beg; lc < end; lc++) { if (!nzA(lc)) nbeg = lc; else break; }
+        for (lc = end; lc >= beg; lc--) if (nzA(lc)) break;
+        nend = lc + 2 < ncol ? lc + 2 : ncol;
+        const int sb = is16 ? nbeg : beg, se = is16 ? nend : end;
+        S newhead = head; bool runToEnd = false;
+        {
+            S l512 = L::wrap(sb); bool tb = true; int lc2;
+            for (lc2 = sb; lc2 < se; lc2++) { bool z = ex && !nzA(lc2); if (!z) break; l512 = L::wrap(l512 + 1); if (z && tb) newhead = l512; tb = z && tb; }
+            runToEnd = ex && (lc2 >= se) && se > sb;
+        }
+        S index = tail; bool runToBot = false;
+        {
+            S l512 = L::wrap(se); bool tb = true; int lc2;
+            for (lc2 = se; lc2 >= sb; lc2--) { bool z = ex && !nzA(lc2); if (!z) break; l512 = L::wrap(l512 - 1); if (z && tb) index = l512; tb = z && tb; }
+            runToBot = ex && lc2 < sb;
+        }
+        if (ex && i + 1 < nrow) {
+            if (runToEnd && !(se <= end && Hh[se] != 0)) FL(256, i);
+            if (runToBot) FL(512, i);
+            const int los = is16 ? 0 : lo;
+            const bool nzsb = nzA(sb);
+            int nhlo, nhhi;
+            if (nzsb) { nhlo = hlo; nhhi = hhi; } else { nhlo = nhhi = newhead; }
+            if (sb > los) {
+                int Pl = -1;
+                if (is16) { if (fzMin < sb) Pl = std::min(fzMax, sb - 1); }
+                else { if (fzMax >= lo) Pl = fzMax; }
+                if (nzsb && Pl < sb - 1) { nhlo = std::min(nhlo, sb); nhhi = std::max(nhhi, sb); }
+                if (Pl >= 0) { nhlo = std::min({nhlo, hlo, los}); nhhi = std::max({nhhi, hhi, Pl}); }
+            }
+            const int Smax = is16 ? std::min(Emax + 2, CMAX) : Emax;
+            int rlo, rhi;
+            if (nzA(se)) { rlo = tlo; rhi = thi; } else { rlo = rhi = index; }
+            if (Smax > se) {
+                const int Qr = firstRightNZ(std::max(se, end), Smax);
+                if (nzA(se)) { rlo = std::min(rlo, se); rhi = std::max(rhi, se); }
+                if (Qr >= 0) { rlo = std::min({rlo, tlo, Qr}); rhi = std::max({rhi, thi, Smax - 1}); }
+            }
+            auto T2 = [&](int r) { int v = r + 2; return v < (int)qlen ? v : (int)qlen; };
+            tlo = T2(rlo); thi = T2(rhi);
+            hlo = nhlo; hhi = nhhi;
+        } else {
+            hlo = hhi = newhead;
+            { S ix = L::wrap(index + 2); tlo = thi = ix < qlen ? ix : qlen; }
+        }
+        head = newhead;
+        { S ix = L::wrap(index + 2); tail = ix < qlen ? ix : qlen; }
+        if (hlo > head) hlo = head; if (hhi < head) hhi = head;
+        if (tlo > tail) tlo = tail; if (thi < tail) thi = tail;
+        if (!ex) break;
+    }
+    p->score = maxScore; p->tle = x; p->qle = y; p->max_off = max_off; p->gscore = gscore; p->gtle = max_ie;
+    return flag;
+}
+
 Params unpack(const int32_t *pp) {
     Params P;
     P.o_del = pp[0]; P.e_del = pp[1]; P.o_ins = pp[2]; P.e_ins = pp[3];
@@ -623,6 +898,25 @@ int oracle_bsw_scalar(const int32_t *params, int32_t *pairs, int64_t n,
         total += c;
     });
     if (cells_out) *cells_out = total.load();
+    return 0;
+}
+
+
+// The library's group-coupling detector (see detect_pair): every pair scored
+// alone; outputs into pairs[0, n), flags[k] != 0 where pair k's outputs may
+// depend on its SIMD group.  Returns 0, or -1 on bad arguments.
+int oracle_bsw_detect(const int32_t *params, int bits, int32_t *pairs, int64_t n,
+                      const uint8_t *ref, const uint8_t *qer, int32_t w, int32_t *flags,
+                      int nthreads) {
+    if (!params || !pairs || !flags || n < 0 || (bits != 8 && bits != 16)) return -1;
+    Params P = unpack(params);
+    if (P.e_del <= 0 || P.e_ins <= 0) return -1;
+    Pair *pp = (Pair *)pairs;
+    parallel_groups(n, nthreads, [&](int64_t s, int64_t e) {
+        for (int64_t k = s; k < e; k++)
+            flags[k] = bits == 16 ? detect_pair<int16_t>(P, pp + k, ref, qer, w)
+                                  : detect_pair<int8_t>(P, pp + k, ref, qer, w);
+    });
     return 0;
 }
 
