@@ -16,7 +16,8 @@ _lib = None
 def build(force=False):
     srcs = [os.path.join(HERE, "emu.cpp"), os.path.join(HERE, "fake", "cuda_runtime.h"),
             os.path.join(CSRC, "bsw_kernel.cuh"), os.path.join(CSRC, "bsw_lane.cuh"),
-            os.path.join(CSRC, "sw_kernel.cuh"), os.path.join(CSRC, "bsw_group.cuh")]
+            os.path.join(CSRC, "sw_kernel.cuh"), os.path.join(CSRC, "bsw_group.cuh"),
+            os.path.join(CSRC, "bsw_couple.cuh")]
     if force or not os.path.exists(SO) or os.path.getmtime(SO) < max(os.path.getmtime(s) for s in srcs):
         os.makedirs(os.path.dirname(SO), exist_ok=True)
         subprocess.check_call(["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-pthread", "-w",
@@ -47,6 +48,32 @@ def run(pairs, ref, qer, w, params, bits=16, K=4, warps=1, wpair=None, G=32, win
                      None if wp is None else vp(wp.ctypes.data), int(bits), vp(kp.ctypes.data),
                      int(G), int(K), int(warps), int(win), ctypes.byref(ef), ctypes.byref(ei))
     return out, ef.value, ei.value
+
+
+def run_detect(pairs, ref, qer, w, params, bits=16, K=4, warps=1, G=32, win=0):
+    """run() with the group-coupling detector on; returns (pairs, err_flags,
+    sorted indices of the flagged pairs)."""
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+    out = np.ascontiguousarray(pairs).copy()
+    kp = np.array([params[k] for k in ("o_del", "e_del", "o_ins", "e_ins", "zdrop", "end_bonus", "a", "b")],
+                  np.int32)
+    ef = ctypes.c_int(0)
+    ei = ctypes.c_longlong(0)
+    nf = ctypes.c_int(0)
+    fl = np.zeros(max(1, out.shape[0]), np.int64)
+    ref = np.ascontiguousarray(ref)
+    qer = np.ascontiguousarray(qer)
+    vp = ctypes.c_void_p
+    rc = _lib.emu_bsw_run_det(vp(out.ctypes.data), vp(ref.ctypes.data), ctypes.c_longlong(0),
+                              ctypes.c_longlong(ref.shape[0]), vp(qer.ctypes.data), ctypes.c_longlong(0),
+                              ctypes.c_longlong(qer.shape[0]), int(out.shape[0]), int(w), None, int(bits),
+                              vp(kp.ctypes.data), int(G), int(K), int(warps), int(win), ctypes.byref(ef),
+                              ctypes.byref(ei), vp(fl.ctypes.data), ctypes.byref(nf), int(fl.shape[0]))
+    assert rc == 0, "divergent warp exit"
+    idx = np.sort(fl[: nf.value] & 0xffffffff).astype(np.int64)
+    return out, ef.value, idx
 
 
 def run_group(pairs, ref, qer, w, params, bits=16, warps=2, ref_lo=0, qer_lo=0):

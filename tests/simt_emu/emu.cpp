@@ -119,6 +119,31 @@ extern "C" int emu_bsw_run(talbsw::DevPair *pairs, const uint8_t *ref, long long
     return run_launch(A, G, K, warps);
 }
 
+// The same with the group-coupling detector on: flagged pairs are appended
+// to flagged[0, cap) ((request + 1) << 32 | pair), their count to *nflagged.
+extern "C" int emu_bsw_run_det(talbsw::DevPair *pairs, const uint8_t *ref, long long ref_lo,
+                               long long ref_hi, const uint8_t *qer, long long qer_lo,
+                               long long qer_hi, int n, int w, const int32_t *wpair, int bits,
+                               const int32_t *kp, int G, int K, int warps, int win, int *err_flags,
+                               long long *err_index, long long *flagged, int *nflagged, int cap) {
+    talbsw::LaunchArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.pairs = pairs;
+    A.ref = ref; A.ref_lo = ref_lo; A.ref_hi = ref_hi;
+    A.qer = qer; A.qer_lo = qer_lo; A.qer_hi = qer_hi;
+    A.wpair = wpair;
+    A.n = n; A.w = w; A.bits = bits; A.win = win;
+    int m1 = 1, m2 = 1;
+    for (int i = 0; i < n; i++) { m1 = std::max(m1, pairs[i].len1); m2 = std::max(m2, pairs[i].len2); }
+    A.cols_cap = m2; A.rows_cap = m1;
+    int counter = 0;
+    *err_flags = 0; *err_index = (long long)INT64_MAX; *nflagged = 0;
+    A.work_counter = &counter; A.err_flags = err_flags; A.err_index = err_index;
+    A.flagged = flagged; A.nflagged = nflagged; A.flag_cap = cap;
+    A.P = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], kp[6], kp[7]};
+    return run_launch(A, G, K, warps);
+}
+
 // The grouped kernel (the reference's SIMD groups, one warp each) over n
 // pairs with one band; `warps` warps share the groups.
 extern "C" int emu_bsw_group_run(talbsw::DevPair *pairs, const uint8_t *ref, long long ref_lo,

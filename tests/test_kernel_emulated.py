@@ -361,3 +361,40 @@ def test_emulated_lane_kernel_on_coupled_fixtures_scores_pairs_alone(f):
     assert ef == 0
     alone = oracle.vector(p, d["ref"], d["qer"], w, P, bits=bits, lanes=1)
     assert (outputs(got) == outputs(alone)).all()
+
+
+def _detector_cases():
+    from test_coupling_detector import _adversarial
+    cases = []
+    for seed in range(6):
+        p, ref, qer, w, P, bits = _adversarial(9100 + seed)
+        if p.shape[0]:
+            cases.append((f"adv{seed}", p[:90], ref, qer, w, P, bits))
+    for f in COUPLED + [os.path.join(GOLDEN, n) for n in ("wl_c2_16bit.npz", "edge16_band_3.npz",
+                                                            "edge8_band_17.npz", "edge16_zdrop_1.npz")]:
+        d = np.load(f)
+        P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+        cases.append((os.path.basename(f), d["inputs"][:90], d["ref"], d["qer"], int(d["w"]), P,
+                      int(d["bits"])))
+    return cases
+
+
+@pytest.mark.parametrize("G,K,ring", [(1, 4, False), (1, 4, True), (8, 4, False), (8, 4, True), (32, 2, False)])
+@pytest.mark.parametrize("case", _detector_cases(), ids=lambda c: c[0])
+def test_emulated_detector_flags_equal_oracle(case, G, K, ring):
+    """The kernels' group-coupling detector (bsw_couple.cuh inside the lane
+    and G-lane kernels) flags exactly the pairs its CPU restatement flags,
+    and scores every other pair as the oracle does alone."""
+    name, p, ref, qer, w, P, bits = case
+    win = 0
+    if ring:  # row rings as the launches size them: a multiple of 32 (lane) / a power of two
+        win = (2 * w + 12 + 31) & ~31 if G == 1 else 1 << max(6, (2 * w + 11).bit_length())
+        if win >= int(p["len2"].max()) + 4:
+            pytest.skip("whole rows are smaller than the ring")
+    got, ef, idx = simt_emu.run_detect(p, ref, qer, w, P, bits=bits, K=K, G=G, warps=2, win=win)
+    assert ef == 0
+    one, flags = oracle.detect(p, ref, qer, w, P, bits=bits)
+    want = np.nonzero(flags)[0]
+    assert idx.tolist() == want.tolist()
+    keep = np.setdiff1d(np.arange(p.shape[0]), want)
+    assert (outputs(got)[keep] == outputs(one)[keep]).all()

@@ -59,7 +59,7 @@ struct DevPair {  // SeqPair, bandedSWA.h:90-99
 
 // error word layout: bit 0 = domain error seen; the first offending pair
 // index is recorded separately with atomicMin.
-enum : int { ERR_DOMAIN = 1, ERR_CAPACITY = 2, ERR_BASE = 4 };
+enum : int { ERR_DOMAIN = 1, ERR_CAPACITY = 2, ERR_BASE = 4, ERR_FLAGCAP = 8 };
 
 // One request of a serving tick: the tick's pairs are the concatenation of
 // its requests' pair arrays, each request with its own sequence buffers,
@@ -104,7 +104,30 @@ struct LaunchArgs {
     // pairs / ref / qer / wpair / w / bits above are unused
     ReqDesc *reqs;
     const int32_t *order_req;
+    // group-coupling detector (bsw_couple.cuh): when `flagged` is set, the
+    // kernels flag every pair whose outputs may depend on its SIMD group (or
+    // that lies outside their exact range but inside the grouped kernel's),
+    // append it as ((request + 1) << 32) | pair to flagged[0, flag_cap) and
+    // leave its outputs to the grouped re-scoring; when it is not set, such
+    // pairs are scored alone (or refused, outside the range)
+    long long *flagged = nullptr;
+    int *nflagged = nullptr;
+    int flag_cap = 0;
 };
+
+// Appends a flagged pair to the launch's list.
+__device__ __forceinline__ void flag_pair(const LaunchArgs &A, int req, int pidx) {
+    const int k = atomicAdd(A.nflagged, 1);
+    if (k < A.flag_cap) A.flagged[k] = ((long long)(req + 1) << 32) | (unsigned)pidx;
+    else atomicOr(A.err_flags, ERR_FLAGCAP);
+}
+
+// Is the pair inside the grouped kernel's range (the reference's own limits:
+// lengths up to the element type's, h0 >= 0; any gap weights)?
+__device__ __forceinline__ bool pair_in_group_range(int len1, int len2, int h0, int w, bool is8) {
+    const int lim = is8 ? 127 : 32767;
+    return len1 >= 0 && len2 >= 0 && len1 <= lim && len2 <= lim && h0 >= 0 && w >= 0;
+}
 
 // Where one pair's record, sequences, band and precision live.
 struct PairSrc {
@@ -456,6 +479,12 @@ __device__ __forceinline__ int scan_last_nz(const int *Hh, const int *Fv, int lo
     return found;
 }
 
+}  // namespace talbsw
+
+#include "bsw_couple.cuh"
+
+namespace talbsw {
+
 // Per-pair state, uniform across the pair's G lanes.
 struct PairState {
     DevPair *pp;
@@ -469,6 +498,7 @@ struct PairState {
     int sh, msk;  // element width: wrap shift and unsigned mask
     bool is8;
     unsigned long long ncells;
+    Couple cp;  // group-coupling detector state (uniform over the pair's lanes)
 };
 
 template <int G, int K>
@@ -508,6 +538,12 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
     PairState ps;
     ps.pidx = 0; ps.req = -1; ps.pp = nullptr; ps.nrow = 0; ps.ncol = 0; ps.i = 0; ps.ncells = 0;
     bool active = false, done = false;
+    const bool det = A.flagged != nullptr;  // run the group-coupling detector
+    // drops a flagged pair: its group is re-scored by the grouped kernel
+    auto drop = [&]() {
+        if (gl == 0) flag_pair(A, ps.req, ps.pidx);
+        active = false;
+    };
     const int nwork = work_count(A);
     const int32_t *order = A.seg ? A.order + A.seg[0] : A.order;
     const int32_t *order_req = A.reqs ? (A.seg ? A.order_req + A.seg[0] : A.order_req) : nullptr;
@@ -549,15 +585,23 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
                 if (src.bits == 8) is8 = true;
                 else if (src.bits == 16) is8 = false;
                 else is8 = pair_in_range(P, len1, len2, h0in, wcall, true);
-                ok = pair_in_range(P, len1, len2, h0in, wcall, is8) && wcall >= 0 &&
-                     (long long)idr >= src.ref_lo && (long long)idq >= src.qer_lo &&
-                     (long long)idr + len1 <= src.ref_hi && (long long)idq + len2 <= src.qer_hi;
+                const bool inwin = (long long)idr >= src.ref_lo && (long long)idq >= src.qer_lo &&
+                                   (long long)idr + len1 <= src.ref_hi && (long long)idq + len2 <= src.qer_hi;
+                ok = pair_in_range(P, len1, len2, h0in, wcall, is8) && wcall >= 0 && inwin;
                 if (!ok) {
-                    if (gl == 0) report_error(A, req, ERR_DOMAIN, pidx);
+                    // outside the exact range of int32 cells: the grouped
+                    // kernel computes in the element type and takes it
+                    if (gl == 0) {
+                        if (det && inwin && pair_in_group_range(len1, len2, h0in, wcall, is8)) flag_pair(A, req, pidx);
+                        else report_error(A, req, ERR_DOMAIN, pidx);
+                    }
                 } else if (ring ? (2LL * wcall + 12 > A.win && len2 + 4 > A.win)
                                 : (len2 > A.cols_cap)) {
                     ok = false;
-                    if (gl == 0) report_error(A, req, ERR_CAPACITY, pidx);
+                    if (gl == 0) {
+                        if (det) flag_pair(A, req, pidx);
+                        else report_error(A, req, ERR_CAPACITY, pidx);
+                    }
                 }
             }
             const bool st = take && ok;
@@ -608,6 +652,7 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
                 ps.v1 = (ps.h0e > oe_ins) ? wrapS(ps.h0e - oe_ins, sh) : 0;
                 ps.initc = 0;
                 ps.fend = 0; ps.p = -1;
+                ps.cp.init(ps.qlenE, ps.v1, P.e_ins);
                 active = true;
             }
             __syncwarp();
@@ -649,18 +694,18 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             }
             __syncwarp();
         }
-        int beg = 0, end = 0, h10init = 0;
+        int beg = 0, end = 0, h10init = 0, hv_next = 0;
         bool changed = false;
         if (rowact) {
             beg = ps.nbeg; end = ps.nend;
             if (beg < i - ps.wk) beg = i - ps.wk;
             if (end > i + ps.wk + 1) end = i + ps.wk + 1;
             if (end > ps.ncol) end = ps.ncol;
-            // column -1 value: H_v[i+1] (:3065-3067)
-            if (beg == 0) {
+            // column -1 value: H_v[i+1] (:3065-3067); DUMMY1 past the last row (:2821-2825)
+            {
                 const int k = i + 1;
-                if (k == ps.nrow) h10init = 99;  // DUMMY1 past the last row (:2821-2825)
-                else h10init = imax(wrapS(ps.h0e - ps.o_delE - k * ps.e_delE, sh), 0);
+                hv_next = (k == ps.nrow) ? 99 : imax(wrapS(ps.h0e - ps.o_delE - k * ps.e_delE, sh), 0);
+                if (beg == 0) h10init = hv_next;
             }
             // per-pair band (:3080-3089)
             const int phead = ps.head, ptail = ps.tail;
@@ -669,6 +714,25 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             t = imin(t, wrapU(ps.qlenE, msk));
             ps.tail = wrapS(t, sh);
             changed = ps.head != phead || ps.tail != ptail;
+            if (det) ps.cp.clamp(wrapS(i - ps.bandE, sh), wrapU(i1 + ps.bandE, msk), wrapU(ps.qlenE, msk), sh, msk);
+        }
+        // group-coupling detector: frozen columns, the row's scalar checks and
+        // the old entries a group may trim
+        if (det) {
+            const bool fz = rowact && ps.cp.frozenTo < beg;
+            const int f0 = scan_first_nz<G>(Hh, Fv, ps.cp.frozenTo, beg, fz, gl, gshift, gbits, wm);
+            const int f1 = scan_last_nz<G>(Hh, Fv, ps.cp.frozenTo, beg - 1, fz, gl, gshift, gbits, wm);
+            if (fz && f0 < beg) { ps.cp.frozen_nz(f0); ps.cp.frozen_nz(f1); }
+            if (rowact) ps.cp.frozenTo = imax(ps.cp.frozenTo, beg);
+            const bool stay = rowact && !(i1 > ps.mlen || ps.tail == ps.head || ps.head > ps.tail);
+            if (rowact)
+                ps.cp.row_checks(true, i1 > ps.mlen, stay, i, ps.wk, beg, end, ps.ncol, h10init, hv_next,
+                                 ps.is8 ? 127 : 32767);
+            const int th = stay ? ps.cp.trim_hi(changed, end, ps.head) : -1;
+            const int ft = scan_first_nz<G>(Hh, Fv, beg, th, stay && beg < th, gl, gshift, gbits, wm);
+            if (stay && beg < th && ft < th) ps.cp.flag |= CPL_TRIM;
+            if (rowact && ps.cp.flag) { drop(); rowact = false; }
+            __syncwarp();
         }
         // columns that left the band since the last row are frozen: note the
         // first nonzero one at or after nbeg (16-bit head re-derivation)
@@ -694,8 +758,10 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
         // score table of this row's target base: byte q of {thi:tlo} is
         // S(t, q) as a signed byte for query code q (0..3 bases, 4 = N)
         RowState r;
+        int tbrow = 0;
         {
             const int tb = rowact ? tnext : 0;
+            tbrow = tb;
             if (rowact && i + 1 < ps.nrow) tnext = Tg[i + 1];
             if (rowact && tb > 4) {  // a target base code above 4
                 if (gl == 0) report_error(A, ps.req, ERR_BASE, ps.pidx);
@@ -711,6 +777,16 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
                 r.tlo = (r.tlo & ~(0xffu << (8 * tb))) | (mat << (8 * tb));
             }
             r.thi = 0x000000ffu;      // N in the query: -1
+        }
+        if (det && rowact) {  // F the group could store differently at the tail column and band end
+            const int tl = ps.tail;
+            const bool tin = tl >= beg && tl < end;
+            int ftl = 0, fen = 0;
+            if (tin) ftl = Couple::fnext(Hh[tl & wm], Fv[tl & wm], prmt_sext(r.tlo, r.thi, Qs[tl & wm]), P.e_del, cc.oe_del);
+            if (end < ps.ncol && end == tl)
+                fen = Couple::fnext(Hh[end & wm], Fv[end & wm], prmt_sext(r.tlo, r.thi, Qs[end & wm]), P.e_del, cc.oe_del);
+            ps.cp.f_checks(true, i, ps.wk, beg, end, ps.head, tl, ps.ncol, ps.is8 ? 127 : 32767, tin, ftl, fen);
+            if (ps.cp.flag) { drop(); rowact = false; }
         }
         r.beg = beg; r.end = end; r.head = ps.head; r.tail = ps.tail;
         r.carryP = -P.e_ins;          // makes E(beg) = 0
@@ -752,6 +828,8 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
                 Hh[jl & wm] = m ? 0 : h10;
                 Fv[jl & wm] = 0;
             }
+            if (det) ps.cp.stored_last(jl, ps.ncol, m ? 0 : h10, tbrow >= 4 ? -1 : -P.b, ps.head, ps.tail,
+                                       P.e_del, cc.oe_del);
             // gscore at the query's last column (:3177-3195); it is in the
             // band exactly when end == ncol, and then it is column end-1
             if (ran && end == ps.ncol && !(ps.qlenE > ps.tail)) {
@@ -815,17 +893,31 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
             // stops inside the band
             const int L2 = scan_last_nz<G>(Hh, Fv, imax(B, beg), E, rowact && E >= B, gl, gshift, gbits, wm);
             if (rowact && ring && E >= B && L2 < beg) {  // would have read a reused ring slot
-                if (gl == 0) report_error(A, ps.req, ERR_CAPACITY, ps.pidx);
-                active = false;
+                if (det) drop();
+                else {
+                    if (gl == 0) report_error(A, ps.req, ERR_CAPACITY, ps.pidx);
+                    active = false;
+                }
                 rowact = false;
             }
             if (rowact) {
                 if (E > B && f2 > B) ps.head = wrapS(f2, sh);
                 int index = ps.tail;
                 if (E >= B && L2 != E) index = L2;
+                const int index0 = index;
                 index = wrapS(index + 2, sh);
                 ps.tail = index < ps.qlenE ? index : ps.qlenE;
                 ps.i = i + 1;
+                if (det) {
+                    const bool last_row = i + 1 >= ps.nrow;
+                    const bool nz_sb = B < beg ? ps.p == B : (Hh[B & wm] | Fv[B & wm]) != 0;
+                    const int hse = Hh[E & wm], fse = Fv[E & wm];
+                    ps.cp.scans(true, last_row, ps.is8, i, ps.wk, beg, end, B, E, nz_sb, (hse | fse) != 0,
+                                E > B && f2 >= E, hse != 0, E >= B && L2 < imax(B, beg), ps.head, index0,
+                                ps.qlenE, ps.ncol, ps.is8 ? 127 : 32767);
+                    ps.cp.settle(true, last_row, ps.head, ps.tail);
+                    if (ps.cp.flag) drop();
+                }
             }
         }
     }

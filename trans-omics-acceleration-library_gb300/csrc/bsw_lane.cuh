@@ -144,6 +144,7 @@ struct LanePair {
     int h0e, v1, wk, bandE, qlenE, mlen, zdropE, sh, msk;
     bool is8;
     unsigned long long ncells;
+    Couple cp;  // group-coupling detector state
 };
 
 // V bit 0: plain group loop (else explicit prefetch of the next group);
@@ -180,6 +181,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
 
     LanePair s = {};
     bool active = false;
+    const bool det = A.flagged != nullptr;  // run the group-coupling detector
     const int nwork = work_count(A);
     const int32_t *order = A.seg ? A.order + A.seg[0] : A.order;
     const int32_t *order_req = A.reqs ? (A.seg ? A.order_req + A.seg[0] : A.order_req) : nullptr;
@@ -213,12 +215,19 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             if (src.bits == 8) is8 = true;
             else if (src.bits == 16) is8 = false;
             else is8 = pair_in_range(P, len1, len2, h0in, wcall, true);
-            const bool ok = pair_in_range(P, len1, len2, h0in, wcall, is8) && wcall >= 0 &&
-                            (long long)idr >= src.ref_lo && (long long)idq >= src.qer_lo &&
-                            (long long)idr + len1 <= src.ref_hi && (long long)idq + len2 <= src.qer_hi;
-            if (!ok) { fail(ERR_DOMAIN, req, pidx); continue; }
+            const bool inwin = (long long)idr >= src.ref_lo && (long long)idq >= src.qer_lo &&
+                               (long long)idr + len1 <= src.ref_hi && (long long)idq + len2 <= src.qer_hi;
+            const bool ok = pair_in_range(P, len1, len2, h0in, wcall, is8) && wcall >= 0 && inwin;
+            if (!ok) {
+                // outside the exact range of int32 cells: the grouped kernel
+                // computes in the element type and takes it
+                if (det && inwin && pair_in_group_range(len1, len2, h0in, wcall, is8)) flag_pair(A, req, pidx);
+                else fail(ERR_DOMAIN, req, pidx);
+                continue;
+            }
             if (A.win > 0 ? (2LL * wcall + 12 > A.win && len2 + 4 > A.win) : (len2 > A.cols_cap)) {
-                fail(ERR_CAPACITY, req, pidx);
+                if (det) flag_pair(A, req, pidx);
+                else fail(ERR_CAPACITY, req, pidx);
                 continue;
             }
             // per-pair constants (smithWatermanBatchWrapper16/8 set-up)
@@ -263,6 +272,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             s.nbeg = 0; s.nend = len2;
             s.fend = 0; s.p = -1;
             s.tnext = len1 > 0 ? s.t[0] : 0;
+            s.cp.init(s.qlenE, s.v1, e_ins);
             active = true;
         }
         if (s.i >= s.nrow) { finish(); continue; }
@@ -311,10 +321,13 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                     if (hf(c) != 0u) { s.p = c; break; }
             s.fend = imax(s.fend, beg);
         }
-        int h10init = 0;  // H_v[i+1] (:3065-3067)
-        if (beg == 0) {
-            const int k = i + 1;
-            h10init = (k == s.nrow) ? 99 : imax(wrapS(s.h0e - P.o_del - k * P.e_del, sh), 0);
+        // H_v[i+1] (:3065-3067): the first column's value, used when beg == 0
+        const int hv_next = (i + 1 == s.nrow) ? 99 : imax(wrapS(s.h0e - P.o_del - (i + 1) * P.e_del, sh), 0);
+        const int h10init = beg == 0 ? hv_next : 0;
+        if (det) {  // columns frozen since the last row: lowest / highest non-zero
+            for (int c = s.cp.frozenTo; c < beg; c++)
+                if (hf(c) != 0u) s.cp.frozen_nz(c);
+            s.cp.frozenTo = imax(s.cp.frozenTo, beg);
         }
         // per-pair band (:3080-3089) and trimming (:3091-3112)
         const int phead = s.head, ptail = s.tail;
@@ -327,7 +340,21 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         }
         s.head = head;
         s.tail = tail;
-        if (head != phead || tail != ptail) {
+        const bool changed = head != phead || tail != ptail;
+        bool oldnz_masked = false;  // old entries of [beg, head) seen non-zero (untrimmed rows)
+        if (det) {
+            s.cp.clamp(wrapS(i - s.bandE, sh), wrapU(i1 + s.bandE, msk), wrapU(s.qlenE, msk), sh, msk);
+            const bool stay = !(i1 > s.mlen || tail == head || head > tail);
+            s.cp.row_checks(true, i1 > s.mlen, stay, i, s.wk, beg, end, ncol, h10init, hv_next,
+                            s.is8 ? 127 : 32767);
+            if (stay && s.cp.hlo != s.cp.hhi) {  // uncertain head: [beg, max(head, hhi)) before trimming
+                const int hi = s.cp.trim_hi(changed, end, head);
+                for (int l = beg; l < hi; l++)
+                    if (hf(l) != 0u) { s.cp.flag |= CPL_TRIM; break; }
+            }
+            if (s.cp.flag) { flag_pair(A, s.req, s.pidx); active = false; continue; }
+        }
+        if (changed) {
             const int hi = imin(end, head);
             for (int l = beg; l < hi; l++) hf(l) = 0u;
         }
@@ -348,6 +375,22 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             }
         }
         const uint32_t thi = 0x000000ffu;
+        if (det) {  // F the group could store differently at the tail column and at the band end
+            const bool tin = tail >= beg && tail < end;
+            int ft = 0, fe = 0;
+            if (tin) {
+                const uint32_t wv = hf(tail);
+                const uint32_t q = (qs(tail) >> (4 * (tail & 7))) & 0xfu;
+                ft = Couple::fnext((int)(wv & 0xffffu), (int)(wv >> 16), lane_score1(tlo, thi, q), e_del, oe_del);
+            }
+            if (end < ncol && end == tail) {
+                const uint32_t wv = hf(end);
+                const uint32_t q = (qs(end) >> (4 * (end & 7))) & 0xfu;
+                fe = Couple::fnext((int)(wv & 0xffffu), (int)(wv >> 16), lane_score1(tlo, thi, q), e_del, oe_del);
+            }
+            s.cp.f_checks(true, i, s.wk, beg, end, head, tail, ncol, s.is8 ? 127 : 32767, tin, ft, fe);
+            if (s.cp.flag) { flag_pair(A, s.req, s.pidx); active = false; continue; }
+        }
 
         // ---- the band [beg, end): masked left part, clean middle, tail part
         int e = 0, hprev = h10init;
@@ -357,6 +400,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         if (end > beg) s.ncells += (unsigned long long)(end - beg);
         for (int j = beg; j < jA; j++) {
             const uint32_t w = hf(j);
+            oldnz_masked |= w != 0u;
             const uint32_t q = (qs(j) >> (4 * (j & 7))) & 0xfu;
             int f2;
             hprev = lane_cell(w, lane_score1(tlo, thi, q), e, f2, oe_ins, e_ins, oe_del, e_del);
@@ -441,7 +485,13 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         {
             const int jl = ran ? end : beg;
             const bool m = (head > jl) || (jl > tail);
-            if (jl <= ncol + 1) hf(jl) = m ? 0u : ((uint32_t)hprev & 0xffffu);
+            const uint32_t hst = m ? 0u : ((uint32_t)hprev & 0xffffu);
+            if (jl <= ncol + 1) hf(jl) = hst;
+            if (det) {
+                if (!changed && oldnz_masked) s.cp.flag |= CPL_TRIM;  // the group may trim them
+                s.cp.stored_last(jl, ncol, (int)hst, tb >= 4 ? -1 : -P.b, head, tail, e_del, oe_del);
+                if (s.cp.flag) { flag_pair(A, s.req, s.pidx); active = false; continue; }
+            }
         }
         // gscore at the query's last column (:3177-3195): in the band exactly
         // when end == ncol, and then it is column end-1
@@ -485,6 +535,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         {   // per-pair head / tail (:3265-3316; 8-bit: the row's own range :2571-2621)
             const int B = s.is8 ? beg : s.nbeg;
             const int E = s.is8 ? end : s.nend;
+            bool run_end = false, run_bot = false;
             if (E > B) {
                 int l = B;
                 bool found = false;
@@ -493,6 +544,7 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                     else l = imin(beg, E);
                 }
                 if (!found) while (l < E && hf(l) == 0u) l++;
+                run_end = l == E;
                 if (l > B) s.head = wrapS(l, sh);
             }
             int index = s.tail;
@@ -501,15 +553,28 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                 // scan stops inside the band
                 int l = E;
                 while (l >= B && hf(l) == 0u) l--;
+                run_bot = l < B;
                 if (l < beg && W > 0) {  // would have read a ring slot reused since
-                    fail(ERR_CAPACITY, s.req, s.pidx);
+                    if (det) flag_pair(A, s.req, s.pidx);
+                    else fail(ERR_CAPACITY, s.req, s.pidx);
                     active = false;
                     continue;
                 }
                 if (l != E) index = l;
             }
+            const int index0 = index;
             index = wrapS(index + 2, sh);
             s.tail = index < s.qlenE ? index : s.qlenE;
+            if (det) {
+                const bool last_row = i + 1 >= s.nrow;
+                const bool nz_sb = B < beg ? s.p == B : hf(B) != 0u;
+                const uint32_t wse = hf(E);
+                s.cp.scans(true, last_row, s.is8, i, s.wk, beg, end, B, E, nz_sb, wse != 0u, run_end,
+                           (wse & 0xffffu) != 0u, run_bot, s.head, index0, s.qlenE, ncol,
+                           s.is8 ? 127 : 32767);
+                s.cp.settle(true, last_row, s.head, s.tail);
+                if (s.cp.flag) { flag_pair(A, s.req, s.pidx); active = false; continue; }
+            }
         }
         s.i = i + 1;
     }
