@@ -2,18 +2,20 @@
 """Benchmark of the banded Smith-Waterman seed extension on GB300.
 
 Metric: BSW GCUPS (reference cells per second; a cell is one iteration of the
-reference's scalar inner loop, bandedSWA.cpp:175-200) and pairs/s.  A step is
-one pass of the hot path over one batch: at N=1 the 16-bit plain-launch
-workload, 1,000,000 seeded synthetic pairs (query U[100,300] bp, 4% subs +
-0.5% 1-5 bp indels, len1 = len2 + U[0,40], h0 ~ U[30,250], w = 100,
-zdrop = 100), scored with getScores16 semantics.
+reference's scalar inner loop, bandedSWA.cpp:175-200) and pairs/s, batched form
+against the plain launch.  A step is one pass of the hot path over one batch:
+at N=1 the mixed-length workload, 10,000,000 seeded synthetic pairs (query
+length lognormal, median 120, sigma 0.8, clipped to [20, 2000]; errors
+U[1%,8%]; band per pair in {20, 50, 100}; h0 U[19,250]; each pair 8- or
+16-bit by the routing rule), scored by the batched form, bit-exact against the
+reference's getScores8 / getScores16.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-`value` is measured with the inputs resident in HBM (device-resident call,
-CUDA events on the library's stream); `e2e` goes through the reference-facing
-C ABI call (tal_bsw_scores) with pinned host buffers, host<->device copies
-inside the timed region.  Under torchrun each rank scores its own shard of
+`value` is measured with the inputs resident in HBM (device-resident batched
+call, CUDA events on the library's stream); `e2e` goes through the C ABI call
+tal_bsw_scores_batched with pinned host buffers, host<->device copies inside
+the timed region.  Under torchrun each rank scores its own shard of
 pairs (independent pairs, no collective): weak scaling.
 """
 from __future__ import annotations
@@ -47,7 +49,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="c2_16bit")
+    ap.add_argument("--workload", default="c3_mixed")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="CPU work for the cpu_baseline sample (rank 0, N=1)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -57,6 +59,7 @@ def parse_args():
                     help="score only the first N pairs of the workload (profiling a small case)")
     ap.add_argument("--no-grouped", action="store_true",
                     help="skip the grouped-form (TAL_BSW_GROUPED) leg")
+    ap.add_argument("--no-extras", action="store_true", help="skip the single-shape workloads")
     ap.add_argument("--no-mixed", action="store_true",
                     help="skip the mixed-length plain-vs-batched comparison")
     ap.add_argument("--mixed-pairs", type=int, default=None,
@@ -224,36 +227,68 @@ def profile_traffic(name):
 
 
 # ---------------------------------------------------------------------- CPU baseline
-def cpu_score(batch, wl, nthreads):
-    """Times the CPU implementation on `batch`; returns (seconds, ref-cells,
-    kind, description).  The reference itself where it was compiled on this
-    host (x86 with AVX-512: getScores16 from oracle/_ref, one instance per
-    thread), else the oracle's port of scalarBandedSWAWrapper (the
-    reference's portable path, equal to getScores16 at e_del = e_ins = 1)."""
+def _classes(batch, wl):
+    """(w, bits, indices) of each call the reference's caller would issue for
+    `batch`: one band per call, 8/16-bit by the routing rule."""
     import oracle
     P = wl.params()
-    bits = 8 if wl.bits == 8 else 16
+    n = batch.n
+    warr = batch.w.astype(np.int64) if wl.w_choices else np.full(n, wl.w, np.int64)
+    if wl.bits in (8, 16):
+        is8 = np.full(n, wl.bits == 8)
+    else:
+        is8 = oracle.eligible8(batch.pairs, warr, P)
+    out = []
+    for wv in np.unique(warr):
+        for bits in (8, 16):
+            sel = np.nonzero((warr == wv) & (is8 == (bits == 8)))[0]
+            if sel.size:
+                out.append((int(wv), bits, sel))
+    return out
+
+
+def cpu_score(batch, wl, nthreads):
+    """Times the CPU implementation on `batch` (one call per band / precision
+    class, as the reference's caller issues them); returns (seconds,
+    ref-cells, kind, description, scored pairs).  The reference itself where
+    it was compiled on this host (x86 with AVX-512: getScores8/16 from
+    oracle/_ref, one instance per thread), else the oracle's port of
+    scalarBandedSWAWrapper (the reference's portable path, equal to
+    getScores16 at e_del = e_ins = 1 and to getScores8 inside the 8-bit
+    range)."""
+    import oracle
+    P = wl.params()
+    out = batch.pairs.copy()
+    cells = 0
     if oracle.ref_available("avx512"):
-        parts = np.array_split(np.arange(batch.n), nthreads)
         t = time.perf_counter()
-        with cf.ThreadPoolExecutor(nthreads) as ex:
-            list(ex.map(lambda ix: oracle.reference(batch.pairs[ix], batch.ref, batch.qer,
-                                                    wl.w, P, mode=bits, pristine=False), parts))
+        for wv, bits, sel in _classes(batch, wl):
+            parts = np.array_split(sel, nthreads)
+            with cf.ThreadPoolExecutor(nthreads) as ex:
+                res = list(ex.map(lambda ix: oracle.reference(batch.pairs[ix], batch.ref, batch.qer,
+                                                              wv, P, mode=bits, pristine=False), parts))
+            for ix, r in zip(parts, res):
+                out[ix] = r
         dt = time.perf_counter() - t
-        _, cells = oracle.scalar(batch.pairs, batch.ref, batch.qer, wl.w, P, nthreads=nthreads)
-        return dt, cells, "reference", f"getScores{bits} (AVX-512BW build of the reference)"
+        for wv, bits, sel in _classes(batch, wl):
+            cells += oracle.scalar(batch.pairs[sel], batch.ref, batch.qer, wv, P, nthreads=nthreads)[1]
+        return dt, cells, "reference", "getScores8/16 (AVX-512BW build of the reference)", out
     t = time.perf_counter()
-    _, cells = oracle.scalar(batch.pairs, batch.ref, batch.qer, wl.w, P, nthreads=nthreads)
+    for wv, bits, sel in _classes(batch, wl):
+        o, c = oracle.scalar(batch.pairs[sel], batch.ref, batch.qer, wv, P, nthreads=nthreads)
+        out[sel] = o
+        cells += c
     dt = time.perf_counter() - t
-    return dt, cells, "port", "oracle port of scalarBandedSWAWrapper (bandedSWA.cpp:116-260)"
+    return dt, cells, "port", "oracle port of scalarBandedSWAWrapper (bandedSWA.cpp:116-260)", out
 
 
 def cpu_sample(wl, seconds, nthreads, first=0):
-    """A batch of the workload sized for about `seconds` of CPU work."""
+    """The first pairs of the workload (the generator is prefix-stable: pair k
+    is the same in any batch size), about `seconds` of CPU work."""
     from tal_bsw import synth
     n = 2000
     probe = synth.generate(wl, n, first=first)
-    dt, cells, _, _ = cpu_score(probe, wl, nthreads)
+    dt = cpu_score(probe, wl, nthreads)[0]
     rate = n / max(dt, 1e-3)
     n2 = int(min(wl.n_pairs, max(n, rate * seconds)))
     return synth.generate(wl, n2, first=first)
@@ -273,8 +308,25 @@ def cpu_isa():
     return f"{m} {model}".strip()
 
 
+def workload_desc(wl, n):
+    """The workload string both arms report (same configuration)."""
+    if wl.name == "c3_mixed":
+        return (f"c3_mixed: {n} pairs, lognormal query (median 120, sigma 0.8) in [20,2000], "
+                "errors U[1%,8%] (80% subs, 20% 1-5 bp indels), w per pair in {20,50,100}, "
+                "h0 U[19,250], 8/16-bit routed per pair (getScores8 / getScores16 semantics), "
+                "batched form vs plain launch")
+    bits = 8 if wl.bits == 8 else 16
+    return (f"{wl.name}: {n} pairs, query U[{wl.len_lo},{wl.len_hi}], w={wl.w}, zdrop={wl.zdrop}, "
+            f"getScores{bits}")
+
+
 # -------------------------------------------------------------------------- our arm
 def run_ours(args):
+    """Headline: the batched mixed-length workload (10,000,000 pairs), the
+    batched form device-resident (`value`) and through tal_bsw_scores_batched
+    on pinned host buffers (`e2e`), beside the plain launch on the same
+    pairs; then the single-shape workloads, the grouped kernel, the sibling
+    kernels, serving and the CPU baseline."""
     import torch
     import tal_bsw
     from tal_bsw import synth
@@ -288,7 +340,8 @@ def run_ours(args):
     first = rank * n                       # each rank its own shard of pairs
     b = synth.generate(wl, n, first=first)
     P = wl.params()
-    bits = 8 if wl.bits == 8 else 16
+    bits = wl.bits                          # 0: 8/16-bit routed per pair
+    wpair = b.w.astype(np.int32) if wl.w_choices else None
     cinfo = workload_cells(wl.name)
 
     bsw = tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
@@ -298,22 +351,24 @@ def run_ours(args):
     dp = torch.from_numpy(pairs_u8.copy()).cuda()
     dr = torch.from_numpy(b.ref).cuda()
     dq = torch.from_numpy(b.qer).cuda()
+    dw = torch.from_numpy(wpair).cuda() if wpair is not None else None
+    dwp = dw.data_ptr() if dw is not None else None
     torch.cuda.synchronize()
 
-    def step_device():
-        bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
-                          n, wl.w, bits)
+    def step_batched():
+        bsw.scores_batched_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                                  n, wl.w, bits, dwp)
 
+    log("batched form: warm-up (autotune, graph capture)")
     for _ in range(max(args.warmup, 3)):
-        step_device()
+        step_batched()
     kernel_cells = bsw.last_cells
-    # ref-cells of this shard: counted once per workload (rank 0's shard is
-    # the workload itself); other shards scale the kernel's own count
+    flagged, regroups = bsw.last_regroup()
     counted = bool(cinfo) and rank == 0 and cinfo["n_pairs"] == n
     ratio = dist.max(int(cinfo["ref_cells"]) / max(kernel_cells, 1) if counted else 0.0)
     ref_cells = int(cinfo["ref_cells"]) if counted else int(kernel_cells * (ratio or 1.0))
 
-    # ---- device-resident timed region
+    # ---- device-resident timed region (the batched form)
     clocks = ClockSampler(local)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -324,15 +379,12 @@ def run_ours(args):
     time.sleep(0.3)
     e0.record(stream)
     t0 = time.perf_counter()
-    kernel_ms = 0.0
     for _ in range(args.steps):
-        step_device()
-        kernel_ms += bsw.last_kernel_ms     # the scoring kernel alone (events around it)
+        step_batched()
     e1.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
-    kernel_s = kernel_ms / 1e3 / args.steps
     launches = bsw.launch_count - launches0
     dist.barrier()
     t_step = e0.elapsed_time(e1) / 1e3 / args.steps
@@ -340,143 +392,124 @@ def run_ours(args):
     total_cells = dist.sum(float(ref_cells))
     total_pairs = n * ws
     value = total_cells / t_step_max / 1e9
+    gpu_out = dp.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE).copy()
+    log(f"batched, device-resident: {value:.1f} GCUPS, {total_pairs / t_step_max / 1e6:.2f} M pairs/s")
 
-    # ---- end to end through the C ABI, host buffers pinned
-    log(f"device-resident: {value:.1f} GCUPS; end-to-end leg")
-    if args.no_e2e:
-        print(json.dumps({"value": value, "unit": UNIT, "ms_per_step": t_step_max * 1e3,
-                          "pairs": n, "gpu_launches": launches}), flush=True)
-        bsw.close()
-        dist.close()
-        return
-    hp = torch.empty(pairs_u8.shape[0], dtype=torch.uint8, pin_memory=True)
-    hr = torch.empty(b.ref.shape[0], dtype=torch.uint8, pin_memory=True)
-    hq = torch.empty(b.qer.shape[0], dtype=torch.uint8, pin_memory=True)
-    hp.numpy()[:] = pairs_u8
-    hr.numpy()[:] = b.ref
-    hq.numpy()[:] = b.qer
-    hpairs = hp.numpy().view(tal_bsw.SEQPAIR_DTYPE)
-    e2e_steps = args.e2e_steps or max(3, args.steps // 2)
-    for _ in range(2):
-        bsw.getScores16(hpairs, hr.numpy(), hq.numpy(), n, 1, wl.w) if bits == 16 else \
-            bsw.getScores8(hpairs, hr.numpy(), hq.numpy(), n, 1, wl.w)
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        if bits == 16:
-            bsw.getScores16(hpairs, hr.numpy(), hq.numpy(), n, 1, wl.w)
-        else:
-            bsw.getScores8(hpairs, hr.numpy(), hq.numpy(), n, 1, wl.w)
-    t_e2e = (time.perf_counter() - t0) / e2e_steps
-    t_e2e_max = dist.max(t_e2e)
-    e2e_value = total_cells / t_e2e_max / 1e9
-    lens = int(b.pairs["len1"].sum() + b.pairs["len2"].sum())
-    h2d = pairs_u8.nbytes + int(b.pairs["len1"].sum()) + int(b.pairs["len2"].sum())
-    d2h = pairs_u8.nbytes
-    # parity guard on the timed outputs: device-resident and host paths agree
-    dev_out = dp.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE)
-    agree = bool((tal_bsw.outputs(dev_out) == tal_bsw.outputs(hpairs)).all())
+    # ---- end to end through the C ABI (tal_bsw_scores_batched), pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        hp = torch.empty(pairs_u8.shape[0], dtype=torch.uint8, pin_memory=True)
+        hr = torch.empty(b.ref.shape[0], dtype=torch.uint8, pin_memory=True)
+        hq = torch.empty(b.qer.shape[0], dtype=torch.uint8, pin_memory=True)
+        hp.numpy()[:] = pairs_u8
+        hr.numpy()[:] = b.ref
+        hq.numpy()[:] = b.qer
+        hw = None
+        if wpair is not None:
+            hw = torch.empty(n, dtype=torch.int32, pin_memory=True)
+            hw.numpy()[:] = wpair
+        hpairs = hp.numpy().view(tal_bsw.SEQPAIR_DTYPE)
 
-    # ---- batched form on the same pairs (device-resident)
-    log("batched form")
+        def step_e2e():
+            bsw.scores_batched(hpairs, hr.numpy(), hq.numpy(), n, wl.w,
+                               wpair=None if hw is None else hw.numpy(), bits=bits)
+        e2e_steps = args.e2e_steps or max(3, args.steps // 2)
+        for _ in range(2):
+            step_e2e()
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            step_e2e()
+        t_e2e_max = dist.max((time.perf_counter() - t0) / e2e_steps)
+        h2d = pairs_u8.nbytes + b.ref.nbytes + b.qer.nbytes + (0 if wpair is None else wpair.nbytes)
+        agree = bool((tal_bsw.outputs(gpu_out) == tal_bsw.outputs(hpairs)).all())
+        e2e = {"value": round(total_cells / t_e2e_max / 1e9, 3), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(pairs_u8.nbytes),
+               "pairs_per_s": round(total_pairs / t_e2e_max, 1), "ms_per_step": round(t_e2e_max * 1e3, 3),
+               "steps": e2e_steps, "outputs_match_device_path": agree,
+               "call": "tal_bsw_scores_batched (host buffers, pinned; copies inside the timed region)"}
+        del hp, hr, hq
 
-    def step_batched():
-        bsw.scores_batched_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
-                                  n, wl.w, bits)
-    for _ in range(max(args.warmup, 3)):
-        step_batched()
-    dist.barrier()
-    torch.cuda.synchronize()
-    b0 = time.perf_counter()
-    for _ in range(args.steps):
-        step_batched()
-    torch.cuda.synchronize()
-    t_batched = dist.max((time.perf_counter() - b0) / args.steps)
-    batched = {"value": round(total_cells / t_batched / 1e9, 3), "unit": UNIT,
-               "pairs_per_s": round(total_pairs / t_batched, 1),
-               "ms_per_step": round(t_batched * 1e3, 3),
-               "segments": segment_configs(bsw),
-               "note": "device-resident batched call (sort into segments = length bin x band "
-                       "class, one persistent launch per segment on forked streams, one CUDA "
-                       "graph); segments: [lanes per pair, columns per lane, max query, row ring]; "
-                       "wall time per synchronous call"}
+    # ---- plain launch (one scoring launch per call) on the same pairs
+    plain = None
+    if not args.no_mixed:
+        log("plain launch on the same pairs")
 
-    # ---- grouped form (the reference's SIMD groups, exact on any input) on
-    # the same pairs: its speed, and how many pairs' outputs differ from the
-    # per-pair kernels' (pairs whose outputs depend on their group)
-    grouped = None
-    if not args.no_grouped:
-        log("grouped form")
-        gbits = bits | tal_bsw.api.GROUPED
-
-        def step_grouped():
+        def step_plain():
             bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
-                              n, wl.w, gbits)
-        step_grouped()
-        gout = dp.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE)
-        ndiff = int((tal_bsw.outputs(gout) != tal_bsw.outputs(dev_out)).any(1).sum())
-        gsteps = 2
+                              n, wl.w, bits, dwp)
+            bsw.sync()
+        step_plain()
+        pflag = bsw.last_regroup()
         dist.barrier()
         torch.cuda.synchronize()
-        g0 = time.perf_counter()
-        gk = 0.0
-        for _ in range(gsteps):
-            step_grouped()
-            gk += bsw.last_kernel_ms
-        torch.cuda.synchronize()
-        t_grouped = dist.max((time.perf_counter() - g0) / gsteps)
-        grouped = {"value": round(total_cells / t_grouped / 1e9, 3), "unit": UNIT,
-                   "ms_per_step": round(t_grouped * 1e3, 3),
-                   "kernel_ms_per_launch": round(gk / gsteps, 3),
-                   "pairs_differing_from_per_pair": dist.sum(ndiff),
-                   "note": "device-resident call with TAL_BSW_GROUPED (one warp per SIMD group of "
-                           "the reference, wrapping int16/int8 values); wall time per synchronous "
-                           "call"}
+        t0 = time.perf_counter()
+        psteps = 2
+        for _ in range(psteps):
+            step_plain()
+        t_plain = dist.max((time.perf_counter() - t0) / psteps)
+        pout = dp.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE)
+        plain = {"value": round(total_cells / t_plain / 1e9, 3), "unit": UNIT,
+                 "pairs_per_s": round(total_pairs / t_plain, 1), "ms_per_step": round(t_plain * 1e3, 2),
+                 "steps": psteps, "flagged_pairs": pflag[0], "regrouped_groups": pflag[1],
+                 "outputs_match_batched": bool((tal_bsw.outputs(pout) == tal_bsw.outputs(gpu_out)).all())}
 
-    # ---- rooflines
+    # ---- rooflines: integer pipe (DPX) and HBM
     hbm_peak, peak_src = measured_peaks()
-    alg_bytes = lens + 56 * n + 24 * n          # bases read, SeqPair read, outputs written
-    achieved = alg_bytes / (kernel_s if kernel_s > 0 else t_step) / 1e9
+    lens = int(b.pairs["len1"].sum() + b.pairs["len2"].sum())
+    alg_bytes = lens + 56 * n + 24 * n + (4 * n if wpair is not None else 0)
     dpx, i32 = probe_int_peak(local)
     int_cells_peak = dpx / 4.0                   # 8 int16 lane-ops per cell, 2 lanes per DPX op
-    # reference cells per second of the scoring kernel alone (this rank)
-    kernel_rate = ref_cells / kernel_s if kernel_s > 0 else value * 1e9 / ws
+    cell_rate = ref_cells / t_step               # this rank, whole batched graph
+    hbm_rate = alg_bytes / t_step / 1e9
 
     result = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": max(args.warmup, 3),
         "ms_per_step": round(t_step_max * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int16", "data": "synthetic (seeded generator, no dataset)",
-        "config": {"workload": f"{wl.name}: {n} pairs, query U[{wl.len_lo},{wl.len_hi}], "
-                               f"w={wl.w}, zdrop={wl.zdrop}, getScores{bits} plain launch",
-                   "pairs_per_step": total_pairs, "ref_cells_per_step": int(total_cells),
-                   "kernel_cells_per_step": int(kernel_cells) * ws,
+        "vs_baseline": None, "dtype": "int16 / int8 (routed per pair), integer DP",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": workload_desc(wl, wl.n_pairs), "pairs_per_step": total_pairs,
+                   "ref_cells_per_step": int(total_cells), "kernel_cells_per_step": int(kernel_cells) * ws,
+                   "call": "tal_bsw_scores_batched_device (device-resident), one CUDA graph per call",
                    "l2": "inputs larger than L2 (no flush needed)",
                    "parallelism": f"replica shards x{ws}, no collective"},
         "pairs_per_s": round(total_pairs / t_step_max, 1),
         "wall_s_timed": round(wall, 3),
-        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "pairs_per_s": round(total_pairs / t_e2e_max, 1),
-                "ms_per_step": round(t_e2e_max * 1e3, 3), "outputs_match_device_path": agree},
+        "exactness": {"flagged_pairs": flagged, "regrouped_groups": regroups,
+                      "flag_rate": round(flagged / max(n, 1), 8),
+                      "note": "pairs whose outputs could depend on their SIMD group (or outside the "
+                              "per-pair kernels' exact range), re-scored in the reference's grouping "
+                              "inside the timed call"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm_peak,
-                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 5),
-                     "kernel_ms_per_launch": round(kernel_s * 1e3, 3),
-                     "traffic": profile_traffic(wl.name), "peak_source": peak_src,
-                     "note": "integer-pipe bound kernel; see roofline_int"},
-        "roofline_int": {"bound": "int (DPX 16x2)", "achieved": round(kernel_rate, 1),
-                         "peak": round(int_cells_peak, 1), "unit": "cells/s",
-                         "frac": round(kernel_rate / int_cells_peak, 5),
-                         "peak_dpx_instr_per_s": dpx, "peak_i32_instr_per_s": i32,
-                         "model": "4 DPX int16x2 instructions per cell (probe measured live)"},
+        "roofline": {"bound": "int16x2 DPX (integer pipe)", "achieved": round(cell_rate, 1),
+                     "peak": round(int_cells_peak, 1), "unit": "cells/s",
+                     "frac": round(cell_rate / int_cells_peak, 5),
+                     "traffic": profile_traffic("c3_mixed_batched"),
+                     "peak_source": "live __viaddmax_s16x2 probe (tal_bsw_probe_int_peak)",
+                     "peak_dpx_instr_per_s": dpx, "peak_i32_instr_per_s": i32,
+                     "model": "4 DPX int16x2 instructions per cell; achieved = reference cells / "
+                              "device time of the batched call (all its launches)"},
+        "roofline_hbm": {"bound": "hbm", "achieved": round(hbm_rate, 2), "peak": hbm_peak,
+                         "unit": "GB/s", "frac": round(hbm_rate / hbm_peak, 6), "peak_source": peak_src,
+                         "algorithmic_bytes_per_step": int(alg_bytes)},
         "clocks": clk,
-        "batched": batched,
     }
-    if grouped:
-        result["grouped"] = grouped
-    if not args.no_mixed:
-        log("mixed-length plain vs batched")
-        result["mixed"] = run_mixed(args, bsw, dist)
+    if e2e:
+        result["e2e"] = e2e
+    if plain:
+        result["plain"] = plain
+        result["batched_over_plain_pairs_per_s"] = round(result["pairs_per_s"] / plain["pairs_per_s"], 2)
+    gpu_keep = gpu_out if rank == 0 else None
+    del dp, dr, dq, dw, b
+    torch.cuda.empty_cache()
+    if not args.no_extras:
+        for name in ("c1_151bp", "c1_8bit", "c2_16bit", "c4_long"):
+            log(f"workload {name}")
+            result[name] = run_workload(name, bsw, dist, args)
+    if not args.no_grouped:
+        log("grouped kernel (TAL_BSW_GROUPED) on c2_16bit")
+        result["grouped"] = run_grouped(bsw, dist)
     if not args.no_full_sw:
         log("unbanded Smith-Waterman")
         result["full_sw"] = run_full_sw(args, dist)
@@ -488,7 +521,7 @@ def run_ours(args):
         result["extend"] = run_extend(args, dist)
     if not args.no_serving:
         log("serving loop")
-        peak = result.get("mixed", {}).get("batched", {}).get("pairs_per_s")
+        peak = result["pairs_per_s"] if wl.name == "c3_mixed" else None
         if args.serve_peak > 0:
             peak = args.serve_peak * dist.ws
         result["serving"] = run_serving(args, dist, peak / dist.ws if peak else None)
@@ -496,61 +529,107 @@ def run_ours(args):
         log("cpu baseline")
         nthreads = os.cpu_count() or 1
         sample = cpu_sample(wl, args.cpu_seconds, nthreads)
-        dt, cells, kind, desc = cpu_score(sample, wl, nthreads)
+        dt, cells, kind, desc, cout = cpu_score(sample, wl, nthreads)
+        m = sample.n
+        match = bool((tal_bsw.outputs(cout) == tal_bsw.outputs(gpu_keep[:m])).all())
         result["cpu_baseline"] = {"value": round(cells / dt / 1e9, 4), "unit": UNIT,
                                   "cores": nthreads, "kind": kind,
-                                  "sample": f"{sample.n} of the {n} pairs (same seeded workload), "
-                                            f"{desc}, {cpu_isa()}",
-                                  "seconds": round(dt, 2)}
+                                  "sample": f"the first {m} of the {n} pairs (the generator is prefix-"
+                                            f"stable), {desc}, {cpu_isa()}",
+                                  "pairs_per_s": round(m / dt, 1), "seconds": round(dt, 2)}
+        result["outputs_match_cpu_baseline"] = match
     bsw.close()
     dist.close()
     if rank == 0:
         print(json.dumps(result), flush=True)
 
 
-def run_mixed(args, bsw_unused, dist):
-    """The mixed-length workload (10,000,000 pairs: lognormal query lengths
-    clipped to [20, 2000], bands 20/50/100 per pair, 8/16-bit routing per
-    pair): plain launch vs batched form on the same device-resident pairs."""
+def run_workload(name, bsw, dist, args):
+    """A single-shape workload, device-resident: the plain launch (its
+    scoring kernel's time and the whole call) and the batched form, in
+    GCUPS, with the pairs flagged for group re-scoring."""
     import torch
     import tal_bsw
     from tal_bsw import synth
-    wl = synth.C3
-    n = args.mixed_pairs or wl.n_pairs
+    wl = synth.WORKLOADS[name]
+    n = wl.n_pairs
     b = synth.generate(wl, n, first=dist.rank * n)
     P = wl.params()
-    bsw = tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
-                                   P["end_bonus"], None, P["a"], P["b"], 1, device=dist.local)
+    bits = wl.bits
+    cinfo = workload_cells(name)
+    w = synth.WORKLOADS[name].w
+    x = tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                 P["end_bonus"], None, P["a"], P["b"], 1, device=dist.local)
     dp = torch.from_numpy(b.pairs.view(np.uint8).reshape(-1).copy()).cuda()
     dr = torch.from_numpy(b.ref).cuda()
     dq = torch.from_numpy(b.qer).cuda()
-    dw = torch.from_numpy(b.w.astype(np.int32)).cuda()
-    del b
-    out = {"workload": f"c3_mixed: {n} pairs, lognormal query (median 120, sigma 0.8) in [20,2000], "
-                       "w per pair in {20,50,100}, 8/16-bit routed per pair"}
-    for mode, steps in (("plain", 2), ("batched", 5)):
+    out = {"workload": workload_desc(wl, n)}
+    steps = 2 if name == "c4_long" else 5
+    for mode in ("plain", "batched"):
         def go():
             if mode == "plain":
-                bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
-                                  n, 100, 0, dw.data_ptr())
+                x.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(), n, w, bits)
+                x.sync()
             else:
-                bsw.scores_batched_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(),
-                                          dq.numel(), n, 100, 0, dw.data_ptr())
-        go()
+                x.scores_batched_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                                        n, w, bits)
+        for _ in range(2):
+            go()
+        fl = x.last_regroup()
+        kcells = x.last_cells
+        cells = int(cinfo["ref_cells"]) if cinfo and cinfo["n_pairs"] == n and dist.rank == 0 else kcells
         dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        kms = 0.0
         for _ in range(steps):
             go()
-        torch.cuda.synchronize()
+            kms += x.last_kernel_ms
         t = dist.max((time.perf_counter() - t0) / steps)
-        cells = dist.sum(float(bsw.last_cells))
-        out[mode] = {"pairs_per_s": round(n * dist.ws / t, 1), "ms_per_step": round(t * 1e3, 2),
-                     "kernel_gcups": round(cells / t / 1e9, 2), "steps": steps}
-    out["batched_over_plain_pairs_per_s"] = round(out["batched"]["pairs_per_s"] /
-                                                  out["plain"]["pairs_per_s"], 2)
-    bsw.close()
+        rec = {"value": round(dist.sum(float(cells)) / t / 1e9, 2), "unit": UNIT,
+               "pairs_per_s": round(n * dist.ws / t, 1), "ms_per_step": round(t * 1e3, 3),
+               "flagged_pairs": fl[0], "regrouped_groups": fl[1]}
+        if mode == "plain":
+            rec["kernel_ms"] = round(kms / steps, 3)
+            rec["kernel_gcups"] = round(cells / (kms / steps / 1e3) / 1e9, 2) if kms > 0 else None
+        out[mode] = rec
+    x.close()
     return out
+
+
+def run_grouped(bsw_unused, dist):
+    """The grouped kernel alone (TAL_BSW_GROUPED: every pair in the
+    reference's SIMD groups) on the 1,000,000-pair 16-bit workload."""
+    import torch
+    import tal_bsw
+    from tal_bsw import synth
+    wl = synth.C2
+    n = wl.n_pairs
+    b = synth.generate(wl, n, first=dist.rank * n)
+    P = wl.params()
+    cinfo = workload_cells(wl.name)
+    x = tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                 P["end_bonus"], None, P["a"], P["b"], 1, device=dist.local)
+    dp = torch.from_numpy(b.pairs.view(np.uint8).reshape(-1).copy()).cuda()
+    dr = torch.from_numpy(b.ref).cuda()
+    dq = torch.from_numpy(b.qer).cuda()
+    gb = 16 | tal_bsw.api.GROUPED
+
+    def go():
+        x.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(), n, wl.w, gb)
+        x.sync()
+    go()
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        go()
+    t = dist.max((time.perf_counter() - t0) / 2)
+    x.close()
+    return {"workload": workload_desc(wl, n), "value": round(int(cinfo["ref_cells"]) / t / 1e9, 2),
+            "unit": UNIT, "ms_per_step": round(t * 1e3, 3),
+            "note": "device-resident call with TAL_BSW_GROUPED (one warp per SIMD group of the "
+                    "reference for every pair); the default path runs it only for flagged pairs"}
 
 
 def run_serving(args, dist, peak_pairs_per_s):
@@ -909,13 +988,15 @@ def run_extend(args, dist):
 
 # -------------------------------------------------------------------- reference arm
 def run_reference(args):
+    """The reference's CPU implementation of the path on this host's cores, on
+    the same workload (`config.workload` as our arm's); each step a bounded
+    sample of it (the first pairs, prefix-stable generator)."""
     from tal_bsw import synth
     ws, rank, _ = dist_info()
     if rank != 0:
         return
     wl = synth.WORKLOADS[args.workload]
     nthreads = os.cpu_count() or 1
-    # each step: a bounded sample of the workload, a few seconds of CPU work
     per_step = max(1.0, min(6.0, 150.0 / max(args.steps + args.warmup, 1)))
     sample = cpu_sample(wl, per_step, nthreads)
     for _ in range(args.warmup):
@@ -923,21 +1004,21 @@ def run_reference(args):
     tot_t, tot_c = 0.0, 0
     kind = desc = ""
     for _ in range(args.steps):
-        dt, cells, kind, desc = cpu_score(sample, wl, nthreads)
+        dt, cells, kind, desc, _ = cpu_score(sample, wl, nthreads)
         tot_t += dt
         tot_c += cells
     value = tot_c / tot_t / 1e9
-    bits = 8 if wl.bits == 8 else 16
     res = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": round(tot_t / args.steps * 1e3, 3), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "int16",
+           "scaling": "weak", "vs_baseline": None, "dtype": "int16 / int8 (routed per pair), integer DP",
            "data": "synthetic (seeded generator, no dataset)", "impl": "reference",
-           "config": {"workload": f"{wl.name}: {wl.n_pairs} pairs, w={wl.w}, getScores{bits}; "
-                                  f"each step a {sample.n}-pair sample"},
+           "config": {"workload": workload_desc(wl, wl.n_pairs), "sample_pairs_per_step": sample.n,
+                      "same_config": True},
            "pairs_per_s": round(sample.n * args.steps / tot_t, 1),
            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nthreads, "kind": kind,
-                            "sample": f"{sample.n} pairs per step, {desc}, {cpu_isa()}"},
+                            "sample": f"the first {sample.n} pairs of the workload per step, {desc}, "
+                                      f"{cpu_isa()}"},
            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(res), flush=True)

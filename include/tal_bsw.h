@@ -41,20 +41,22 @@ enum {
     TAL_BSW_8 = 8,    /* getScores8  (bandedSWA.h:257-262) */
     TAL_BSW_16 = 16,  /* getScores16 (bandedSWA.h:285-290) */
     /* OR into TAL_BSW_8 / TAL_BSW_16 for tal_bsw_scores and
-     * tal_bsw_scores_device (one band per call, no d_w): score the pairs in
+     * tal_bsw_scores_device (one band per call, no d_w): score every pair in
      * the reference's own SIMD groups -- 64 (8-bit) / 32 (16-bit) consecutive
      * pairs of the array, the AVX-512BW widths, the last group padded as the
-     * reference pads it -- with the band each group shares, so that every
-     * output equals the reference's on any input.  Without it each pair is
-     * scored as if alone in its group: the same outputs except where a pair's
-     * band is narrow next to its group's (bandedSWA.cpp:3235-3316 re-derive a
-     * lane's head and tail from the group's band edges); that never happened
-     * on the benchmark workloads and happens to about 1 pair in 500 of
-     * seed-extension batches at bands 4-8.  Grouped scoring computes every
-     * value in the reference's wrapping int8 / int16, so its exact range is
-     * only len1, len2 <= 127 (8-bit) / 32767 (16-bit) and h0 >= 0; it runs one
-     * warp per group and is several times slower than the per-pair kernels. */
-    TAL_BSW_GROUPED = 0x100
+     * reference pads it -- one warp per group, every value in the
+     * reference's wrapping int8 / int16.  The outputs are the same as
+     * without the flag (the default is exact too, see tal_bsw_scores); the
+     * flag only changes how they are computed, several times slower: for
+     * callers that want the grouped computation for every pair. */
+    TAL_BSW_GROUPED = 0x100,
+    /* OR into TAL_BSW_8 / TAL_BSW_16 / TAL_BSW_AUTO for tal_bsw_scores and
+     * tal_bsw_scores_device: score every pair as if it were alone in its SIMD
+     * group (no coupling detector, no group re-scoring) -- the semantics of
+     * the reference's scalarBandedSWAWrapper (bandedSWA.cpp:242-260), which
+     * scores pairs one at a time; pairs outside the per-pair kernels' exact
+     * range give TAL_EDOMAIN. */
+    TAL_BSW_PER_PAIR = 0x200
 };
 
 /* SeqPair, bandedSWA.h:90-99: 14 x int32 = 56 bytes, fields in this order. */
@@ -94,16 +96,29 @@ int tal_bsw_destroy(tal_bsw_handle h);
  * device, scores them, and writes the six outputs back into pairs[0, n).
  * bits: TAL_BSW_8, TAL_BSW_16 or TAL_BSW_AUTO.  w: band, per call.
  *
- * Exact range: 16-bit needs len1, len2 <= 32767, h0 >= 0 and
- * h0 + w_match * min(len1, len2) <= 32767; 8-bit needs len1, len2 <= 127 and
- * h0 + w_match * min(len1, len2) <= 127 (the reference's own 8-bit limits,
- * bandedSWA.h:82 and the int8 score range) plus two no-wrap conditions on
- * the first column and the gap scores.  A pair outside it gives TAL_EDOMAIN
- * (for AUTO: outside both), and no outputs are written.  Capacity: a pair's
- * rows live in shared memory, as a ring of the band's columns (2w + 12 up to
- * 16,384, any query length) or as whole rows (queries up to ~22,000 bases);
- * a pair that fits neither (a query above ~22,000 bases with w above 8,186)
- * also gives TAL_EDOMAIN. */
+ * Exactness: every output equals the reference's.  The reference scores its
+ * array in SIMD groups of 32 (16-bit) / 64 (8-bit) consecutive pairs that
+ * share one band per row, and a pair's outputs can depend on the rest of
+ * its group (bandedSWA.cpp:3235-3316 re-derive a lane's head and tail from
+ * the group's band edges).  The library scores each pair on its own with a
+ * detector that flags every pair whose outputs could depend on its group;
+ * it then re-scores the groups of the flagged pairs in the reference's
+ * grouping, on the device, before the call returns.  With TAL_BSW_AUTO the
+ * grouping is that of the reference's caller: the 8-bit-routed pairs form
+ * one array and the 16-bit-routed ones another, each in array order; with a
+ * band per pair (d_w, wpair) one array per (band, precision).  On the
+ * benchmark workloads about 1 pair in 20,000 is flagged; narrow-band
+ * seed-extension batches flag a few per cent.
+ *
+ * Range: lengths up to 127 (8-bit) / 32767 (16-bit) and h0 >= 0, the
+ * reference's own limits (bandedSWA.h:82).  Pairs whose int8 / int16 values
+ * wrap are scored by the grouped kernel, which wraps as the reference does.
+ * A pair outside the range gives TAL_EDOMAIN (for AUTO: the 8-bit rules are
+ * used where the pair is inside them), and no outputs are written.
+ * Capacity: a pair's rows live in shared memory, as a ring of the band's
+ * columns (2w + 12 up to 16,384, any query length) or as whole rows (queries
+ * up to ~22,000 bases); a call whose pairs fit neither (a query above
+ * ~22,000 bases with w above 8,186) also gives TAL_EDOMAIN. */
 int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufRef,
                    const uint8_t *seqBufQer, int32_t numPairs, int32_t w, int bits);
 
@@ -184,6 +199,12 @@ float tal_bsw_last_kernel_ms(tal_bsw_handle h);
  * (bandedSWA.cpp:199). */
 uint64_t tal_bsw_last_cells(tal_bsw_handle h);
 
+/* Pairs the last collected call flagged as possibly depending on their
+ * SIMD group (or outside the per-pair kernels' exact range), and the groups
+ * it re-scored with the reference's grouping for them (see tal_bsw_scores).
+ * Accounting only; no counterpart in the reference. */
+int tal_bsw_last_regroup(tal_bsw_handle h, int64_t *flagged_pairs, int64_t *groups);
+
 /* Measurement utility, no counterpart in the reference: integer-pipe
  * throughput of `device` in thread-instructions per second, for the
  * roofline -- packed 16x2 add-max (DPX) and plain int32. */
@@ -201,13 +222,24 @@ int tal_bsw_probe_int_peak(int device, double *dpx_per_s, double *i32_per_s);
  * would synchronise the device).  Scores numPairs SeqPair records already in
  * device memory, like tal_bsw_scores_device, but needs no handle and calls no
  * allocator: its only scratch is a fixed TAL_BSW_NOALLOC_SCRATCH_BYTES device
- * array inside the library (a control block), and a call whose scratch would
- * not fit is refused with TAL_EDOMAIN.  Runs on `stream` (a cudaStream_t,
- * NULL = default stream) of the current device and returns when the scores
- * are in d_pairs.  The first call on each device resolves the scratch array's
- * device address; make that first call before any stream capture.  All calls
- * on a device share the one array and clear it themselves, so calls that
- * overlap on the GPU (other threads or streams) race: serialise them. */
+ * array inside the library (a control block).  Runs on `stream` (a
+ * cudaStream_t, NULL = default stream) of the current device and returns when
+ * the scores are in d_pairs; it synchronises `stream` twice (to read the
+ * batch's longest sequences, then the status).  The first call on each device
+ * resolves the scratch array's device address; make that first call before
+ * any stream capture.  All calls on a device share the one array and clear
+ * it themselves, so calls that overlap on the GPU (other threads or streams)
+ * race: serialise them.
+ *
+ * Each pair is scored as if alone in its SIMD group: re-scoring the rare
+ * pairs whose outputs depend on their group (what the handle entry points
+ * do, see tal_bsw_scores) needs device memory that grows with the batch, so
+ * this entry point does not; on those pairs its outputs are the pair's own.
+ * Status: TAL_EDOMAIN for a pair outside the per-pair kernels' exact range
+ * (including wrapping values) or with a base code above 4, TAL_ENOMEM for a
+ * pair whose rows do not fit the kernels' shared memory; the offending pair
+ * is not named here (the handle entry points report it through
+ * tal_bsw_last_bad_pair). */
 int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_seq_pair *d_pairs,
                                   const uint8_t *d_ref, size_t ref_bytes,
                                   const uint8_t *d_qer, size_t qer_bytes, int32_t numPairs,

@@ -180,7 +180,7 @@ def routed(pairs: np.ndarray, ref: np.ndarray, qer: np.ndarray, w, params: Dict[
     forces one; bits 0 routes each pair by eligible8().  w may be a scalar or
     a per-pair array (the pairs of each band and precision, in order, form
     one call).  lanes: SIMD group width (default: the reference's 32 / 64;
-    1 scores every pair alone, as the library's per-pair kernels do)."""
+    1 scores every pair alone in its group)."""
     out = np.ascontiguousarray(pairs).copy()
     n = out.shape[0]
     if n == 0:
@@ -327,7 +327,7 @@ def _scored_with_tries(P: np.ndarray, T: np.ndarray, Q: np.ndarray, w: int, para
     """Scores the batch P at band w, then, per pair, again at band w << i
     while its last attempt changed the score (the first always counts) and
     reached max_off >= (band >> 1) + (band >> 2); the last attempt stands."""
-    R = routed(P, T, Q, w, params, bits=0, lanes=1)
+    R = routed(P, T, Q, w, params, bits=0)
     prev = np.full(P.shape[0], -1, np.int64)
     active = np.ones(P.shape[0], bool)
     for i in range(1, max(1, tries)):
@@ -340,7 +340,7 @@ def _scored_with_tries(P: np.ndarray, T: np.ndarray, Q: np.ndarray, w: int, para
         sub = R[go].copy()
         for f in ("score", "tle", "gtle", "qle", "gscore", "max_off"):
             sub[f] = -1
-        R[go] = routed(sub, T, Q, w << i, params, bits=0, lanes=1)
+        R[go] = routed(sub, T, Q, w << i, params, bits=0)
     return R
 
 
@@ -353,8 +353,9 @@ def extend(ref: np.ndarray, reads: np.ndarray, read_off: np.ndarray, seeds: np.n
     with BWA-MEM's band-doubling retries when band_tries > 1.
     Parity unpinned: this stage (BWA-MEM2's mem_chain2aln) is not in the
     reference; the specification is the header's, the pairs are scored by
-    the pinned BSW oracle (`routed`), each pair alone in its SIMD group as
-    the library's extension layer scores them."""
+    the pinned BSW oracle (`routed`) in the reference's SIMD groups: each
+    batch (left, right, every retry) is one getScores call per precision,
+    pairs in batch order, as the library's extension layer issues them."""
     from tal_bsw.seqpair import SEQPAIR_DTYPE
     from tal_bsw.seeddata import REGION_DTYPE
     a = params["a"]

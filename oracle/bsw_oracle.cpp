@@ -674,7 +674,6 @@ int detect_pair(const Params &P, Pair *p, const uint8_t *ref, const uint8_t *qer
         const int lo = std::max(0, i - w);
         const int Emax = std::min(i + w + 1, CMAX);
         if (wasActive && !(i1 > mlen) && tlo <= hhi && thi > hlo) FL(1 << 12, i);
-        bool unmaskedRight = false;
         if (active) {
             if (tlo != thi) FL(1 << 14, i);            // tail uncertainty: flagged
             if (uncH && hhi > end) FL(1 << 13, i);
@@ -684,22 +683,13 @@ int detect_pair(const Params &P, Pair *p, const uint8_t *ref, const uint8_t *qer
             }
             if (uncH && beg >= hlo && beg < hhi && h10init != 0) FL(1 << 13, i);
             if (beg > lo) {
-                const bool anyNZ = fzMax >= lo;
-                if (!anyNZ) {
-                    if (lo == 0 && hlo <= 0 && Hv[i + 1] != 0) FL(2, i);
-                } else if (hlo < beg && tail >= std::max(lo, hlo)) FL(2, i);
-                else {
-                    for (int j = lo; j < beg; j++) {
-                        if (Hh[j] != 0) {
-                            int M = (int)Hh[j] + (int)score(i, j);
-                            if (M - (int)oe_ins - (beg - 1 - j) * (int)e_ins > 0) { FL(4, i); break; }
-                        }
-                    }
-                    if (hlo <= beg && beg <= thi && nzA(beg - 1)) FL(8, i);
-                }
+                // columns [lo, beg) the group may compute: zero inputs give
+                // zero cells, except column 0's stored H_v[i + 1]
+                if (fzMax >= lo) FL(2, i);
+                else if (lo == 0 && hlo <= 0 && Hv[i + 1] != 0) FL(2, i);
             }
             if (end < Emax) {
-                if (end < thi) unmaskedRight = true;
+                if (end < thi) FL(16, i);  // real cells right of the lane's band
                 // stale row-0 values right of everything written, left of Emax
                 const int a = std::max(end, tlo);
                 int c0 = std::max(a, maxEnd) + 1;
@@ -740,13 +730,6 @@ int detect_pair(const Params &P, Pair *p, const uint8_t *ref, const uint8_t *qer
             }
         }
         if (active) {
-            if (unmaskedRight) {
-                bool z = e11 == 0 && oldHhEnd == 0 && oldFEnd == 0;
-                int c0 = std::max(end, maxEnd) + 1;
-                if (z && c0 <= std::min(Emax, len2 - 1) && initA_pos(c0)) z = false;
-                if (len2 - 1 >= end && len2 - 1 < Emax && thi >= len2 && gscore <= 0) z = false;
-                if (!z) FL(16, i);
-            }
             if (tail_in && f21_tail != 0 && (int)tail < Emax) FL(64, i);
             if (end < Emax && end == tail && head <= end && end < len2) {
                 S sbt = score(i, end);

@@ -116,6 +116,13 @@ inline int __reduce_max_sync(unsigned, int v) {
     for (int i = 0; i < 32; i++) r = (int)all[i] > r ? (int)all[i] : r;
     return r;
 }
+inline int __reduce_add_sync(unsigned, int v) {
+    int64_t all[32];
+    simt::gather((int64_t)v, all);
+    int r = 0;
+    for (int i = 0; i < 32; i++) r += (int)all[i];
+    return r;
+}
 inline unsigned __reduce_min_sync(unsigned, unsigned v) {
     int64_t all[32];
     simt::gather((int64_t)v, all);

@@ -132,3 +132,15 @@ def test_precision_constants_match_the_header():
     assert vals["TAL_BSW_16"] == tal_bsw.api.BITS16
     assert vals["TAL_BSW_GROUPED"] == tal_bsw.api.GROUPED
     assert vals["TAL_BSW_GROUPED"] & 0xff == 0
+
+
+def test_cpp_dropin_header_compiles_and_links():
+    """The C++ drop-in header (include/bandedSWA_gb300.h) compiles with g++
+    -Wall -Werror (its SeqPair layout static_asserts included) and a caller of
+    the reference's interface links against libtal_bsw.so.  Running it needs a
+    GB300 (tests/test_gpu_cpp_dropin.py)."""
+    import tempfile
+    import cpp_dropin
+    with tempfile.TemporaryDirectory() as d:
+        exe = cpp_dropin.build(d)
+        assert os.path.exists(exe)

@@ -24,3 +24,6 @@ def test_reference_arm_prints_one_json_line():
     assert cb["value"] == d["value"] and cb["cores"] >= 1 and cb["kind"] in ("reference", "port")
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+    # the same workload as our arm's headline, each step a bounded sample of it
+    assert d["config"]["workload"].startswith("c3_mixed: 10000000 pairs")
+    assert d["config"]["same_config"] is True and d["config"]["sample_pairs_per_step"] > 0

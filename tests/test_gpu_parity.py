@@ -73,8 +73,7 @@ def test_edge_cases(bits):
 
 
 def test_golden_fixtures():
-    files = [f for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
-             if not os.path.basename(f).startswith(("coupled", "wrap"))]
+    files = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
     assert files, "no golden fixtures"
     for f in files:
         d = np.load(f)
@@ -227,18 +226,101 @@ def test_grouped_matches_golden(f):
     _assert_same(d["expected"], got, os.path.basename(f) + " grouped")
 
 
-def test_per_pair_on_coupled_fixtures_scores_pairs_alone():
-    """Without the flag, each pair is scored as if alone in its group: on
-    the coupled fixtures that is the oracle at one lane, which differs from
-    the reference's grouped outputs in a few pairs."""
-    for f in sorted(glob.glob(os.path.join(GOLDEN, "coupled*.npz"))):
+def test_default_path_is_exact_on_coupled_and_wrapping_fixtures():
+    """Without any flag the plain call equals the reference on the fixtures
+    where a pair's outputs depend on its SIMD group (the per-pair kernels
+    flag those pairs and their groups are re-scored in the reference's
+    grouping) and on those whose int8 / int16 values wrap (outside the
+    per-pair kernels' exact range, scored by the grouped kernel)."""
+    files = sorted(glob.glob(os.path.join(GOLDEN, "coupled*.npz")) + glob.glob(os.path.join(GOLDEN, "wrap*.npz")))
+    assert len(files) >= 6
+    for f in files:
         d = np.load(f)
         P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
         bits = int(d["bits"])
-        got = _gpu(d["inputs"], d["ref"], d["qer"], d["w"], P, bits)
-        alone = oracle.vector(d["inputs"], d["ref"], d["qer"], int(d["w"]), P, bits=bits, lanes=1)
-        _assert_same(alone, got, os.path.basename(f) + " per pair")
-        assert (outputs(got) != outputs(d["expected"])).any(1).sum() >= 1
+        with _bsw(P) as bsw:
+            got = d["inputs"].copy()
+            bsw._scores(got, d["ref"], d["qer"], got.shape[0], int(d["w"]), bits)
+            flagged, groups = bsw.last_regroup()
+        _assert_same(d["expected"], got, os.path.basename(f) + " default path")
+        if "coupled" in f:
+            alone = oracle.vector(d["inputs"], d["ref"], d["qer"], int(d["w"]), P, bits=bits, lanes=1)
+            assert (outputs(alone) != outputs(d["expected"])).any(1).sum() >= 1
+            assert flagged >= 1 and groups >= 1
+
+
+def _coupled_mix():
+    """Pairs of the 16- and 8-bit coupled fixtures (same scoring) as one
+    batch: interleaved in runs of 7, bands 4 and 8 per pair.  The expected
+    outputs are the reference's for that batch split as its caller would --
+    one call per (band, precision) class, pairs in array order."""
+    parts = []
+    for name in ("coupled16_band_4.npz", "coupled16_band_8.npz", "coupled8_band_8.npz"):
+        d = np.load(os.path.join(GOLDEN, name))
+        parts.append((d["inputs"], d["ref"], d["qer"], int(d["w"])))
+    P = {k: int(v) for k, v in zip(np.load(os.path.join(GOLDEN, "coupled16_band_4.npz"))["param_keys"],
+                                   np.load(os.path.join(GOLDEN, "coupled16_band_4.npz"))["param_vals"])}
+    refs, qers, rows, ws = [], [], [], []
+    roff = qoff = 0
+    for p, r, q, w in parts:
+        p = p.copy()
+        p["idr"] += roff
+        p["idq"] += qoff
+        refs.append(r); qers.append(q); rows.append(p); ws.append(np.full(p.shape[0], w, np.int32))
+        roff += r.shape[0]; qoff += q.shape[0]
+    pairs = np.concatenate(rows)
+    wpair = np.concatenate(ws)
+    ref, qer = np.concatenate(refs), np.concatenate(qers)
+    rng = np.random.default_rng(17)
+    runs = np.array_split(np.arange(pairs.shape[0]), pairs.shape[0] // 7)
+    order = np.concatenate([runs[k] for k in rng.permutation(len(runs))])
+    pairs, wpair = pairs[order], wpair[order]
+    exp = oracle.routed(pairs, ref, qer, wpair, P, bits=0)
+    return pairs, ref, qer, wpair, P, exp
+
+
+def test_batched_and_device_calls_are_exact_on_coupled_pairs():
+    """The batched form (per-pair bands, 8/16-bit routing) and the
+    device-resident plain call re-score flagged pairs' groups in the grouping
+    the reference's caller would use, so they equal the reference on a
+    batch mixing coupled pairs of both precisions and two bands."""
+    import torch
+    pairs, ref, qer, wpair, P, exp = _coupled_mix()
+    with _bsw(P) as bsw:
+        got = pairs.copy()
+        bsw.scores_batched(got, ref, qer, got.shape[0], w=100, wpair=wpair, bits=0)
+        _assert_same(exp, got, "batched, coupled mix")
+        assert bsw.last_regroup()[1] >= 1
+        dp = torch.from_numpy(pairs.view(np.uint8).reshape(-1).copy()).cuda()
+        dr = torch.from_numpy(ref).cuda()
+        dq = torch.from_numpy(qer).cuda()
+        dw = torch.from_numpy(wpair).cuda()
+        bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                          pairs.shape[0], 100, 0, d_w=dw.data_ptr())
+        bsw.sync()
+        dev = dp.cpu().numpy().view(tal_bsw.SEQPAIR_DTYPE)
+        _assert_same(exp, dev, "device call, coupled mix")
+        # the same again: the pass leaves its tables empty for the next call
+        got2 = pairs.copy()
+        bsw.scores_batched(got2, ref, qer, got2.shape[0], w=100, wpair=wpair, bits=0)
+        _assert_same(exp, got2, "batched, coupled mix, second call")
+
+
+def test_server_is_exact_on_coupled_requests():
+    """Serving: coupled fixtures as requests in one tick, each request its
+    own caller array -- every output equals the reference's."""
+    reqs = []
+    for name in ("coupled16_band_4.npz", "coupled8_band_8.npz", "coupled16_band_8.npz", "wrap16_h0_near_limit_band_100.npz"):
+        d = np.load(os.path.join(GOLDEN, name))
+        reqs.append((d["inputs"].copy(), d["ref"], d["qer"], int(d["w"]), int(d["bits"]), d["expected"]))
+    P = {k: int(v) for k, v in zip(np.load(os.path.join(GOLDEN, "coupled16_band_4.npz"))["param_keys"],
+                                   np.load(os.path.join(GOLDEN, "coupled16_band_4.npz"))["param_vals"])}
+    with _bsw(P) as bsw, tal_bsw.BswServer(bsw, pool_bytes=256 << 20) as srv:
+        tickets = [srv.submit(p, r, q, w=w, bits=b) for p, r, q, w, b, _ in reqs]
+        infos = [srv.poll(t, timeout_us=60_000_000) for t in tickets]
+    for (p, _, _, _, _, e), info, name in zip(reqs, infos, range(len(reqs))):
+        assert info is not None and info.status == tal_bsw.api.TAL_OK
+        _assert_same(e, p, f"server request {name}")
 
 
 @pytest.mark.parametrize("wl,bits,n", [(synth.C2, 16, 3000), (synth.C1_8, 8, 5001), (synth.C4, 16, 70)])
@@ -267,21 +349,6 @@ def test_grouped_device_path_and_chunked_host_call_agree():
     _assert_same(host, dev, "grouped host vs device")
     exp = oracle.vector(b.pairs[:640], b.ref, b.qer, 100, P, bits=8)
     _assert_same(exp, host[:640], "grouped chunk 0 head")
-
-
-def test_wrapping_fixtures_grouped_only():
-    """Gap opens whose int8 sums wrap, and 16-bit scores that wrap past the
-    int16 limit: the per-pair kernels refuse the pairs (outside their exact
-    range), the grouped kernel gives the reference's outputs (checked by
-    test_grouped_matches_golden)."""
-    files = sorted(glob.glob(os.path.join(GOLDEN, "wrap*.npz")))
-    assert len(files) >= 3
-    for f in files:
-        d = np.load(f)
-        P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
-        with pytest.raises(tal_bsw.TalBswError) as ei:
-            _gpu(d["inputs"], d["ref"], d["qer"], d["w"], P, int(d["bits"]))
-        assert ei.value.status == tal_bsw.api.TAL_EDOMAIN
 
 
 def test_grouped_bad_pair_in_a_later_chunk():

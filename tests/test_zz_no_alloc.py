@@ -1,12 +1,15 @@
 """The allocation-free entry point (tal_bsw_scores_device_noalloc), called
 through the C ABI: two calls in a row on device buffers the test owns, each
-compared with the regular entry point (tal_bsw_scores) on the same pairs.
-Integer outputs, so the tolerance is zero.  Collected last on purpose."""
+compared with the regular entry point (tal_bsw_scores) on the same pairs, and
+a slice compared with the oracle scoring each pair alone in its SIMD group
+(the entry point's documented semantics).  Integer outputs, so the tolerance
+is zero.  Collected last on purpose."""
 import ctypes
 
 import numpy as np
 import pytest
 
+import oracle
 import tal_bsw
 from tal_bsw import synth
 from tal_bsw.seqpair import outputs
@@ -50,6 +53,16 @@ def test_noalloc_matches_regular_entry_point(name, bits):
         e, g = outputs(expected), outputs(got)
         bad = np.nonzero((e != g).any(axis=1))[0]
         assert bad.size == 0, f"call {call}: {bad.size} pairs differ, first {bad[0]}"
+    # a slice against the oracle, each pair alone in its group, routed per pair
+    k = slice(0, 300)
+    sub = b.pairs[k]
+    is8 = np.full(sub.shape[0], bits == 8) if bits else oracle.eligible8(sub, w, P)
+    exp = sub.copy()
+    for bb in (8, 16):
+        sel = np.nonzero(is8 == (bb == 8))[0]
+        if sel.size:
+            exp[sel] = oracle.vector(sub[sel], b.ref, b.qer, w, P, bits=bb, lanes=1)
+    assert (outputs(exp) == outputs(got[k])).all(), "noalloc slice differs from the oracle"
 
 
 def test_noalloc_reports_out_of_range_pairs():
@@ -61,6 +74,12 @@ def test_noalloc_reports_out_of_range_pairs():
     d_ref = torch.from_numpy(b.ref).cuda()
     d_qer = torch.from_numpy(b.qer).cuda()
     assert _noalloc(lib, P, d_pairs, d_ref, d_qer, b.n, 100, 8) == tal_bsw.api.TAL_EDOMAIN
+    # a base code above 4 is a domain error too
+    q = b.qer.copy()
+    q[int(b.pairs["idq"][5]) + 1] = 9
+    d_q9 = torch.from_numpy(q).cuda()
+    d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
+    assert _noalloc(lib, P, d_pairs, d_ref, d_q9, b.n, 100, 16) == tal_bsw.api.TAL_EDOMAIN
     # the next call clears the shared control block and succeeds
     d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
     assert _noalloc(lib, P, d_pairs, d_ref, d_qer, b.n, 100, 16) == tal_bsw.api.TAL_OK

@@ -184,6 +184,32 @@ int launch_grouped(tal_bsw_ctx *h, const talbsw::LaunchArgs &A, int slot = 0) {
     return TAL_OK;
 }
 
+// Sizes the regroup arena for a call of n pairs with queries up to max2;
+// captured batched graphs hold its old pointers when it grows.
+int ensure_regroup(tal_bsw_ctx *h, long long n, int max2) {
+    bool grown = false;
+    cudaError_t e = h->regroup.ensure(n, max2, h->num_sms, &grown);
+    if (e != cudaSuccess) return fail(h, TAL_ENOMEM, std::string("regroup buffers: ") + cudaGetErrorString(e));
+    if (grown) {
+        for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second.exec);
+        h->graphs.clear();
+    }
+    return TAL_OK;
+}
+
+// Re-scores the SIMD groups of the pairs a plain launch flagged (A: the
+// call's pairs, windows, band and precision); status into control block 0.
+int launch_regroup(tal_bsw_ctx *h, talbsw::LaunchArgs A) {
+    Ctrl *c = reinterpret_cast<Ctrl *>(h->ctrl.p);
+    A.err_flags = &c->flags;
+    A.err_index = &c->bad_index;
+    A.cells = &c->cells;
+    A.P = h->kp;
+    cudaError_t e = talbsw::enqueue_regroup(h->regroup.V, A, 0, A.n, h->num_sms, h->stream, &h->launches);
+    if (e != cudaSuccess) return cuda_fail(h, e, "regroup launch");
+    return TAL_OK;
+}
+
 // Waits for the launches of control blocks [0, nslots) and merges their
 // status: flags or-ed, the first bad pair (block k's pair indices start at
 // k * per), cells summed.
@@ -208,6 +234,8 @@ int collect_chunks(tal_bsw_ctx *h, int nslots, int32_t per) {
         if (c.flags & talbsw::ERR_DOMAIN) why += "pair outside the exact 8/16-bit range; ";
         if (c.flags & talbsw::ERR_CAPACITY) why += "pair longer than the row capacity; ";
         if (c.flags & talbsw::ERR_BASE) why += "base code above 4; ";
+        if (c.flags & talbsw::ERR_FLAGCAP)
+            why += "more than 1024 band / precision classes among pairs that need group scoring; ";
         return fail(h, TAL_EDOMAIN, why + "first bad pair " + std::to_string(c.bad_index));
     }
     return TAL_OK;
@@ -278,6 +306,7 @@ int tal_bsw_destroy(tal_bsw_handle h) {
         for (DevBuf *b : {&h->xref, &h->xreads, &h->xjobs, &h->xpairs, &h->xtarena, &h->xqarena,
                           &h->xout, &h->xretry, &h->gscratch})
             b->release();
+        h->regroup.release();
         h->bseg.release();
         h->bctrl.release();
         h->btune_seg.release();
@@ -302,9 +331,12 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
     h->last_error.clear();
     h->last_bad = -1;
     const bool grouped = (bits & TAL_BSW_GROUPED) != 0;
-    bits &= ~TAL_BSW_GROUPED;
-    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16) || (grouped && bits == 0))
+    const bool perpair = (bits & TAL_BSW_PER_PAIR) != 0;  // each pair alone: no regrouping
+    bits &= ~(TAL_BSW_GROUPED | TAL_BSW_PER_PAIR);
+    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16) || (grouped && bits == 0) ||
+        (grouped && perpair))
         return fail(h, TAL_EINVAL, "bad numPairs or bits");
+    const bool exact = !grouped && !perpair;  // per-pair kernels + regroup pass
     if (numPairs == 0) return TAL_OK;
     if (!pairs || !seqBufRef || !seqBufQer) return fail(h, TAL_EINVAL, "NULL buffer");
     cudaError_t e = cudaSetDevice(h->device);
@@ -382,6 +414,15 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
             }
         }
     }
+    // exact scoring: a last partial 8-bit group re-scored in the reference's
+    // grouping has padding lanes that read the query bytes at the caller's
+    // offset 0 (the reference pads with zeroed SeqPairs); copy them too
+    // when the windows start within 1 MiB of it
+    if (exact && bits != 16 && all.qlo <= (1 << 20)) {
+        all.qlo = 0;
+        for (int c = 0; c < nch; c++)
+            if (ext[c].qlo <= (1 << 20)) ext[c].qlo = 0;
+    }
     align(all);
     for (int c = 0; c < nch; c++) align(ext[c]);
     // chunk windows that overlap much (pairs sharing sequences) copy once, whole
@@ -392,19 +433,29 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
         ext[0] = all;
         per = numPairs;
     }
-    // device layout: every chunk's windows back to back, 16-byte aligned
-    long long roff[kChunks], qoff[kChunks], rtot = 0, qtot = 0;
+    // device layout: the call's whole window, each chunk's window copied to its
+    // place in it (so any pair -- and the SIMD groups re-scored across chunk
+    // boundaries -- resolves through one window); sparse windows copy as one chunk
+    if (nch > 1 && ((all.rhi - all.rlo) + (all.qhi - all.qlo)) > 2 * sum) {
+        nch = 1;
+        ext[0] = all;
+        per = numPairs;
+    }
+    long long roff[kChunks], qoff[kChunks];
+    const long long rtot = all.rhi - all.rlo, qtot = all.qhi - all.qlo;
     for (int c = 0; c < nch; c++) {
-        roff[c] = rtot;
-        qoff[c] = qtot;
-        rtot += ((ext[c].rhi - ext[c].rlo) + 15) & ~15LL;
-        qtot += ((ext[c].qhi - ext[c].qlo) + 15) & ~15LL;
+        roff[c] = ext[c].rlo - all.rlo;
+        qoff[c] = ext[c].qlo - all.qlo;
     }
     const size_t pbytes = (size_t)numPairs * sizeof(tal_seq_pair);
     if ((e = h->pairs.ensure(pbytes)) != cudaSuccess ||
         (e = h->ref.ensure((size_t)rtot + 16)) != cudaSuccess ||
         (e = h->qer.ensure((size_t)qtot + 16)) != cudaSuccess)
         return fail(h, TAL_ENOMEM, std::string("device buffers: ") + cudaGetErrorString(e));
+    if (exact) {
+        int rc = ensure_regroup(h, numPairs, all.max2);
+        if (rc != TAL_OK) return rc;
+    }
     if (nch > 1 && !h->cstream) {
         e = cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking);
         for (int c = 0; c < kChunks && e == cudaSuccess; c++)
@@ -447,9 +498,13 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
         talbsw::LaunchArgs A;
         memset(&A, 0, sizeof(A));
         A.pairs = reinterpret_cast<talbsw::DevPair *>(dp);
-        A.ref = dr;
-        A.qer = dq;
-        A.ref_lo = ext[c].rlo; A.ref_hi = ext[c].rhi; A.qer_lo = ext[c].qlo; A.qer_hi = ext[c].qhi;
+        A.ref = reinterpret_cast<uint8_t *>(h->ref.p);
+        A.qer = reinterpret_cast<uint8_t *>(h->qer.p);
+        A.ref_lo = all.rlo; A.ref_hi = all.rhi; A.qer_lo = all.qlo; A.qer_hi = all.qhi;
+        if (exact) {
+            talbsw::attach_regroup(A, h->regroup.V);
+            A.flag_base = k0;
+        }
         A.order = nullptr;
         A.wpair = nullptr;
         A.n = k1 - k0;
@@ -459,6 +514,25 @@ int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufR
         A.cols_cap = std::max(all.max2, 1);
         A.rows_cap = std::max(all.max1, 1);
         int rc = grouped ? launch_grouped(h, A, c) : launch_scoring(h, A, w, c);
+        if (rc != TAL_OK) {
+            cudaStreamSynchronize(h->stream);
+            if (h->cstream) cudaStreamSynchronize(h->cstream);
+            return rc;
+        }
+    }
+    // the SIMD groups of flagged pairs, over the whole call (errors into
+    // chunk 0's control block, whose pair indices are the call's)
+    if (exact) {
+        talbsw::LaunchArgs A;
+        memset(&A, 0, sizeof(A));
+        A.pairs = reinterpret_cast<talbsw::DevPair *>(h->pairs.p);
+        A.ref = reinterpret_cast<uint8_t *>(h->ref.p);
+        A.qer = reinterpret_cast<uint8_t *>(h->qer.p);
+        A.ref_lo = all.rlo; A.ref_hi = all.rhi; A.qer_lo = all.qlo; A.qer_hi = all.qhi;
+        A.n = numPairs;
+        A.w = w;
+        A.bits = bits;
+        int rc = launch_regroup(h, A);
         if (rc != TAL_OK) {
             cudaStreamSynchronize(h->stream);
             if (h->cstream) cudaStreamSynchronize(h->cstream);
@@ -568,6 +642,22 @@ int tal_bsw_probe_int_peak(int device, double *dpx_per_s, double *i32_per_s) {
     return TAL_OK;
 }
 
+int tal_bsw_last_regroup(tal_bsw_handle h, int64_t *flagged_pairs, int64_t *groups) {
+    if (!h || !flagged_pairs || !groups) return TAL_EINVAL;
+    std::lock_guard<std::mutex> lk(h->mu);
+    *flagged_pairs = 0;
+    *groups = 0;
+    if (!h->regroup.V.ctr) return TAL_OK;
+    int c[8];
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c, h->regroup.V.ctr, sizeof(c), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "regroup counters");
+    *flagged_pairs = c[6];
+    *groups = c[7];
+    return TAL_OK;
+}
+
 int tal_bsw_scores_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t *d_ref,
                           size_t ref_bytes, const uint8_t *d_qer, size_t qer_bytes,
                           int32_t numPairs, int32_t w, const int32_t *d_w, int bits) {
@@ -576,9 +666,12 @@ int tal_bsw_scores_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t
     h->last_error.clear();
     h->last_bad = -1;
     const bool grouped = (bits & TAL_BSW_GROUPED) != 0;
-    bits &= ~TAL_BSW_GROUPED;
-    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16) || (grouped && (bits == 0 || d_w)))
+    const bool perpair = (bits & TAL_BSW_PER_PAIR) != 0;
+    bits &= ~(TAL_BSW_GROUPED | TAL_BSW_PER_PAIR);
+    if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16) || (grouped && (bits == 0 || d_w)) ||
+        (grouped && perpair))
         return fail(h, TAL_EINVAL, "bad numPairs or bits");
+    const bool exact = !grouped && !perpair;
     if (numPairs == 0) return TAL_OK;
     if (!d_pairs || !d_ref || !d_qer) return fail(h, TAL_EINVAL, "NULL buffer");
     if (((uintptr_t)d_ref & 15) || ((uintptr_t)d_qer & 15))
@@ -611,7 +704,13 @@ int tal_bsw_scores_device(tal_bsw_handle h, tal_seq_pair *d_pairs, const uint8_t
     A.bits = bits;
     A.cols_cap = std::max(hc[1], 1);
     A.rows_cap = std::max(hc[0], 1);
+    if (exact) {
+        int rc = ensure_regroup(h, numPairs, hc[1]);
+        if (rc != TAL_OK) return rc;
+        talbsw::attach_regroup(A, h->regroup.V);
+    }
     int rc = grouped ? launch_grouped(h, A) : launch_scoring(h, A, w);
+    if (rc == TAL_OK && exact) rc = launch_regroup(h, A);
     if (rc != TAL_OK) return rc;
     h->pending_status = TAL_OK;
     return TAL_OK;

@@ -455,6 +455,8 @@ int collect_batch(tal_bsw_ctx *h) {
         if (c.flags & ERR_DOMAIN) why += "pair outside the exact 8/16-bit range; ";
         if (c.flags & ERR_CAPACITY) why += "pair longer than the row capacity; ";
         if (c.flags & ERR_BASE) why += "base code above 4; ";
+        if (c.flags & ERR_FLAGCAP)
+            why += "more than 1024 band / precision classes among pairs that need group scoring; ";
         return bfail(h, TAL_EDOMAIN, why + "first bad pair " + std::to_string(c.bad_index));
     }
     return TAL_OK;
@@ -479,12 +481,17 @@ int batched_device_locked(tal_bsw_ctx *h, tal_seq_pair *d_pairs, const uint8_t *
         (e = h->btune_seg.ensure(sizeof(int) * 2 * kNumSegs)) != cudaSuccess ||
         (e = h->bfork.create()) != cudaSuccess)
         return bfail(h, TAL_ENOMEM, std::string("batched buffers: ") + cudaGetErrorString(e));
-    if (grow) {  // captured graphs hold the old order buffer
+    // the regroup pass's arena: queries up to the 16-bit limit (a captured
+    // graph is replayed on new contents of the same buffers)
+    bool rgrow = false;
+    if ((e = h->regroup.ensure(numPairs, 32767, h->num_sms, &rgrow)) != cudaSuccess)
+        return bfail(h, TAL_ENOMEM, std::string("regroup buffers: ") + cudaGetErrorString(e));
+    if (grow || rgrow) {  // captured graphs hold the old order / regroup buffers
         for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second.exec);
         h->graphs.clear();
     }
     DevPair *pairs = reinterpret_cast<DevPair *>(d_pairs);
-    const LaunchArgs base = base_args(pairs, d_ref, ref_bytes, d_qer, qer_bytes, w, d_w, bits);
+    LaunchArgs base = base_args(pairs, d_ref, ref_bytes, d_qer, qer_bytes, w, d_w, bits);
     if (!h->tuned) {
         int rc = autotune(h, base, numPairs, w);
         if (rc != TAL_OK) return rc;
@@ -497,6 +504,15 @@ int batched_device_locked(tal_bsw_ctx *h, tal_seq_pair *d_pairs, const uint8_t *
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
         cudaGraph_t g = nullptr;
+        // the scoring launches flag pairs whose outputs may depend on their
+        // SIMD group; the regroup pass re-scores those groups exactly
+        attach_regroup(base, h->regroup.V);
+        LaunchArgs rg = base;
+        rg.n = numPairs;
+        rg.err_flags = &handle_sort_bufs(h).ctrl->flags;
+        rg.err_index = &handle_sort_bufs(h).ctrl->bad_index;
+        rg.cells = &handle_sort_bufs(h).ctrl->cells;
+        rg.P = h->kp;
         e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
             cudaError_t e1 = enqueue_sort(h, handle_sort_bufs(h), base, 0, numPairs, h->stream);
@@ -504,6 +520,8 @@ int batched_device_locked(tal_bsw_ctx *h, tal_seq_pair *d_pairs, const uint8_t *
                                  ? enqueue_segs_forked(h, handle_sort_bufs(h), base, nullptr,
                                                        numPairs, w, h->bfork, h->stream, false)
                                  : e1;
+            if (e2 == cudaSuccess)
+                e2 = enqueue_regroup(h->regroup.V, rg, 0, numPairs, h->num_sms, h->stream, &h->launches);
             e = cudaStreamEndCapture(h->stream, &g);
             if (e == cudaSuccess) e = e2;
         }
@@ -515,7 +533,7 @@ int batched_device_locked(tal_bsw_ctx *h, tal_seq_pair *d_pairs, const uint8_t *
         ge.exec = exec;
         it = h->graphs.emplace(key, ge).first;
     } else {
-        h->launches += 4 + kNumSegs;
+        h->launches += 4 + kNumSegs + 10;
     }
     e = cudaGraphLaunch(it->second.exec, h->stream);
     if (e != cudaSuccess) return bfail(h, TAL_ECUDA, std::string("graph launch: ") + cudaGetErrorString(e));

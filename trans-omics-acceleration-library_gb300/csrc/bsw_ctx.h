@@ -113,6 +113,54 @@ struct BatchCtrl {
     unsigned long long cells;
 };
 
+// Arena of the regroup pass (bsw_regroup.cu), which re-scores the SIMD
+// groups of the pairs the per-pair kernels flag: the flagged list (the
+// kernels' LaunchArgs::flagged), the flagged pairs' classes (band,
+// precision, request) in a hash table of kRegroupClasses slots, per-chunk
+// class counts and their scan, the marked groups in a hash table, their
+// members and the grouped kernel's scratch.  ctr: [0] flagged pairs,
+// [1] / [2] marked 16- / 8-bit groups, [3] / [4] grouped-kernel work
+// counters, [5] overflow bits; [6] / [7] the last pass's flagged pairs and
+// re-scored groups.
+constexpr int kRegroupClasses = 1024;  // distinct classes among one call's flagged pairs
+constexpr int kRegroupChunk = 2048;    // pairs per counting chunk
+struct RegroupView {
+    int *ctr = nullptr;
+    long long *flagged = nullptr;
+    int *cls_of = nullptr;
+    long long *gidx = nullptr;
+    unsigned long long *ckeys = nullptr;
+    int4 *cinfo = nullptr;
+    int *counts = nullptr, *offsets = nullptr, *totals = nullptr;
+    unsigned long long *mhash = nullptr;
+    int2 *mlist = nullptr;
+    int *mslot = nullptr;
+    long long *members = nullptr;
+    int4 *ginfo = nullptr;
+    int16_t *scratch = nullptr;
+    int nchunks = 0, fcap = 0, mcap = 0, hcap = 0, col_cap = 0, warps = 0;
+};
+struct RegroupBufs {
+    DevBuf arena;
+    RegroupView V;
+    // Sizes the arena for ntotal pairs with queries up to cols_cap (grow-only;
+    // *grown: the pointers changed, so captured graphs are stale).  Not
+    // while a capture is open: it may allocate and synchronises.
+    cudaError_t ensure(long long ntotal, int cols_cap, int num_sms, bool *grown);
+    void release() { arena.release(); V = RegroupView(); }
+};
+// Enqueues the regroup pass after a scoring launch of A's pairs (ntotal in
+// the launch's pair space; nreq requests when A.reqs is set).  Flags it
+// cannot handle (the tables overflowed) end as ERR_FLAGCAP in A.err_flags.
+cudaError_t enqueue_regroup(const RegroupView &V, LaunchArgs A, int nreq, long long ntotal,
+                            int num_sms, cudaStream_t s, uint64_t *launches);
+// The flagged-list fields of a scoring launch that feeds the pass.
+inline void attach_regroup(LaunchArgs &A, const RegroupView &V) {
+    A.flagged = V.flagged;
+    A.nflagged = V.ctr;
+    A.flag_cap = V.fcap;
+}
+
 struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
 };
@@ -199,6 +247,7 @@ struct tal_bsw_ctx {
     cudaStream_t stream = nullptr;
     talbsw::DevBuf pairs, ref, qer, ctrl, wpair, caps;
     talbsw::DevBuf gscratch;  // grouped scoring: one row slot per warp
+    talbsw::RegroupBufs regroup;  // exact scoring of flagged pairs' SIMD groups
     talbsw::DevBuf porder;  // plain launch: work order by target length, and its buckets
     // seed extension: reference, reads, copy jobs + seeds, pairs, arenas, regions
     talbsw::DevBuf xref, xreads, xjobs, xpairs, xtarena, xqarena, xout, xretry;

@@ -41,7 +41,29 @@ struct GroupArgs {
     int *err_flags;
     long long *err_index;
     KernelParams P;
+    // member mode (re-scoring the groups of flagged pairs, bsw_regroup.cu):
+    // group g's lane l is the pair with global index members[g * 64 + l]
+    // (-1: a padding lane), its band and request are ginfo[g] {w, req,
+    // padding lanes' len2, -}, and the groups are 0 .. *ngroups_dev; a
+    // global index is the pair's index, or its request's `first` plus its
+    // index there when reqs is set (a serving tick's pairs)
+    const long long *members = nullptr;
+    const int4 *ginfo = nullptr;
+    const int *ngroups_dev = nullptr;
+    int ngroups_cap = 1 << 30;
+    ReqDesc *reqs = nullptr;
+    int nreq = 0;
 };
+
+// Global pair index -> (request, local index) in a serving tick's pair space.
+__device__ __forceinline__ int group_req_of(const ReqDesc *reqs, int nreq, long long gi) {
+    int lo = 0, hi = nreq - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (reqs[mid].first <= gi) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
 
 // Lanes per group: 64 for 8-bit, 32 for 16-bit (AVX-512BW SIMD_WIDTH8/16).
 __host__ __device__ inline int group_lanes(int bits) { return bits == 8 ? 64 : 32; }
@@ -82,7 +104,8 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
     uint32_t *HF = reinterpret_cast<uint32_t *>(A.scratch + (size_t)gw * A.slot_elems);
     int8_t *Q2 = reinterpret_cast<int8_t *>(HF + (size_t)A.col_cap * W);
     const KernelParams &P = A.P;
-    const int ngroups = (A.n + W - 1) / W;
+    const bool mm = A.members != nullptr;  // member mode
+    const int ngroups = mm ? imin(*A.ngroups_dev, A.ngroups_cap) : (A.n + W - 1) / W;
 
     // scores and constants (bandedSWA.cpp:50-68), wrapped to the element width
     const int w_match = E::ws((int8_t)P.a);
@@ -106,28 +129,61 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
         // 8-bit: len1 = 0, len2 = the last pair's len2, :2012-2018), h0 = 0
         int len1[LPT], len2[LPT], h0r[LPT];
         long long idr[LPT], idq[LPT];
+        DevPair *pp[LPT];
+        long long lidx[LPT];  // the pair's index in its caller's array (for errors)
         bool real[LPT];
         bool bad = false;
+        // this group's band, sequence windows and request
+        int gw = A.w, greq = -1, padq = 0;
+        DevPair *gpairs = A.pairs;
+        const uint8_t *Aref = A.ref, *Aqer = A.qer;
+        long long ref_lo = A.ref_lo, ref_hi = A.ref_hi, qer_lo = A.qer_lo, qer_hi = A.qer_hi;
+        if (mm) {
+            const int4 gi = A.ginfo[g];
+            gw = gi.x; greq = gi.y; padq = gi.z;
+            if (greq >= 0) {
+                const ReqDesc &d = A.reqs[greq];
+                gpairs = d.pairs;
+                Aref = d.ref; Aqer = d.qer;
+                ref_lo = d.ref_lo; ref_hi = d.ref_hi; qer_lo = d.qer_lo; qer_hi = d.qer_hi;
+            }
+        }
+        auto gerr = [&](int flag, long long k) {
+            atomicOr(A.err_flags, flag);
+            if (greq >= 0) {
+                atomicOr(&A.reqs[greq].err, flag);
+                atomicMin(&A.reqs[greq].bad, k);
+            } else {
+                atomicMin(A.err_index, k);
+            }
+        };
         for (int u = 0; u < LPT; u++) {
-            const long long k = (long long)g * W + t + 32 * u;
-            real[u] = k < A.n;
+            long long k = (long long)g * W + t + 32 * u;
+            if (mm) {
+                k = A.members[(size_t)g * 64 + t + 32 * u];
+                real[u] = k >= 0;
+                if (real[u] && greq >= 0) k -= A.reqs[greq].first;
+            } else {
+                real[u] = k < A.n;
+            }
+            lidx[u] = k;
+            pp[u] = real[u] ? gpairs + k : nullptr;
             if (real[u]) {
-                const DevPair &p = A.pairs[k];
+                const DevPair &p = *pp[u];
                 len1[u] = p.len1; len2[u] = p.len2; h0r[u] = p.h0;
                 idr[u] = p.idr; idq[u] = p.idq;
                 const int lim = is16 ? 32767 : 127;
                 const bool ok = len1[u] >= 0 && len2[u] >= 0 && len1[u] <= lim && len2[u] <= lim &&
-                                h0r[u] >= 0 && idr[u] >= A.ref_lo && idr[u] + len1[u] <= A.ref_hi &&
-                                idq[u] >= A.qer_lo && idq[u] + len2[u] <= A.qer_hi &&
+                                h0r[u] >= 0 && idr[u] >= ref_lo && idr[u] + len1[u] <= ref_hi &&
+                                idq[u] >= qer_lo && idq[u] + len2[u] <= qer_hi &&
                                 len2[u] + 3 <= A.col_cap;
                 if (!ok) {
-                    atomicOr(A.err_flags, ERR_DOMAIN);
-                    atomicMin(A.err_index, k);
+                    gerr(ERR_DOMAIN, k);
                     bad = true;
                 }
             } else {
                 len1[u] = 0;
-                len2[u] = is16 ? 0 : A.pairs[A.n - 1].len2;
+                len2[u] = is16 ? 0 : (mm ? padq : A.pairs[A.n - 1].len2);
                 h0r[u] = 0;
                 idr[u] = idq[u] = -1;
             }
@@ -149,7 +205,7 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
 
         // ---- per-lane set-up: query codes, the first row, band clamp
         int h0[LPT], tlen[LPT], qlen[LPT], myband[LPT];
-        int bsz = A.w;
+        int bsz = gw;
         for (int u = 0; u < LPT; u++) {
             const int l = t + 32 * u;
             h0[u] = E::ws((int)E::us(h0r[u]));
@@ -158,16 +214,15 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
             // a padding lane (8-bit) reads the query bytes at the caller's
             // offset 0, as the reference's zeroed SeqPair does; they only
             // matter where its wrapped first column is non-zero
-            const uint8_t *q = real[u] ? A.qer + (idq[u] - A.qer_lo)
-                             : (A.qer_lo <= 0 && len2[u] <= A.qer_hi) ? A.qer - A.qer_lo : nullptr;
+            const uint8_t *q = real[u] ? Aqer + (idq[u] - qer_lo)
+                             : (qer_lo <= 0 && len2[u] <= qer_hi) ? Aqer - qer_lo : nullptr;
             int tt = (h0[u] > oe_ins) ? E::ws(h0[u] - oe_ins) : 0;
             for (int k = 0; k < colCap; k++) {
                 int code = 0;
                 if (k < len2[u]) {
                     const int b = q ? q[k] : 4;
                     if (b > 4 && real[u]) {
-                        atomicOr(A.err_flags, ERR_BASE);
-                        atomicMin(A.err_index, (long long)g * W + l);
+                        gerr(ERR_BASE, lidx[u]);
                         bad = true;
                     }
                     code = b == 4 ? -1 : E::ws(b);
@@ -187,7 +242,7 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
             int temp = (int)E::us(qlenb + eb_ins);
             int mi = temp / P.e_ins + 1;
             mi = mi > 1 ? mi : 1;
-            myband[u] = E::ws((int)E::us(A.w > mi ? mi : A.w));
+            myband[u] = E::ws((int)E::us(gw > mi ? mi : gw));
             temp = (int)E::us(qlenb + eb_del);
             mi = temp / P.e_del + 1;
             mi = mi > 1 ? mi : 1;
@@ -228,7 +283,7 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
         };
         unsigned long long ncells = 0;
         int tnext[LPT];  // the next row's target base
-        for (int u = 0; u < LPT; u++) tnext[u] = len1[u] > 0 ? A.ref[idr[u] - A.ref_lo] : 0;
+        for (int u = 0; u < LPT; u++) tnext[u] = len1[u] > 0 ? Aref[idr[u] - ref_lo] : 0;
         int beg = 0, end = ncol, nbeg = 0, nend = ncol;
         for (int i = 0; i < nrow; i++) {
             const int i1 = E::ws(i + 1);
@@ -243,12 +298,9 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
                 h10[u] = beg == 0 ? Hv(i + 1, u) : 0;
                 if (i < len1[u]) {
                     const int b = tnext[u];  // loaded a row ahead
-                    if (i + 1 < len1[u]) tnext[u] = A.ref[idr[u] - A.ref_lo + i + 1];
+                    if (i + 1 < len1[u]) tnext[u] = Aref[idr[u] - ref_lo + i + 1];
                     s1[u] = b == 4 ? -1 : E::ws(b);
-                    if (b > 4) {
-                        atomicOr(A.err_flags, ERR_BASE);
-                        atomicMin(A.err_index, (long long)g * W + t + 32 * u);
-                    }
+                    if (b > 4) gerr(ERR_BASE, lidx[u]);
                 } else {
                     s1[u] = 99;  // DUMMY1
                 }
@@ -446,7 +498,7 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
         }
         for (int u = 0; u < LPT; u++) {
             if (!real[u]) continue;
-            DevPair &p = A.pairs[(long long)g * W + t + 32 * u];
+            DevPair &p = *pp[u];
             p.score = maxScore[u];
             p.tle = x[u];
             p.qle = y[u];
@@ -454,10 +506,11 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
             p.gscore = gscore[u];
             p.gtle = max_ie[u];
         }
-        if (t == 0 && A.cells) {
-            int nreal = A.n - g * W;
-            nreal = nreal < W ? nreal : W;
-            atomicAdd(A.cells, ncells * (unsigned long long)nreal);
+        if (A.cells) {
+            int nr = 0;
+            for (int u = 0; u < LPT; u++) nr += real[u];
+            const int nreal = __reduce_add_sync(full, nr);
+            if (t == 0) atomicAdd(A.cells, ncells * (unsigned long long)nreal);
         }
         __syncwarp();
     }

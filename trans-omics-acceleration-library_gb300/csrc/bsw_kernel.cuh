@@ -113,12 +113,13 @@ struct LaunchArgs {
     long long *flagged = nullptr;
     int *nflagged = nullptr;
     int flag_cap = 0;
+    int flag_base = 0;  // added to a flagged pair's index (a chunk of a larger call)
 };
 
 // Appends a flagged pair to the launch's list.
 __device__ __forceinline__ void flag_pair(const LaunchArgs &A, int req, int pidx) {
     const int k = atomicAdd(A.nflagged, 1);
-    if (k < A.flag_cap) A.flagged[k] = ((long long)(req + 1) << 32) | (unsigned)pidx;
+    if (k < A.flag_cap) A.flagged[k] = ((long long)(req + 1) << 32) | (unsigned)(pidx + A.flag_base);
     else atomicOr(A.err_flags, ERR_FLAGCAP);
 }
 

@@ -150,12 +150,16 @@ extern "C" int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_s
     const talbsw::KConfig cfg = talbsw::fit_config(talbsw::choose_config(w, A.cols_cap, A.win),
                                                    A.cols_cap, g_smem_optin[dev], A.win);
     if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap, A.win) > g_smem_optin[dev])
-        return TAL_EDOMAIN;  // a pair too long for the shared-memory rows
+        return TAL_ENOMEM;  // a pair too long for the shared-memory rows
     e = talbsw::launch_config(A, cfg, g_num_sms[dev], g_smem_optin[dev], s);
     if (e != cudaSuccess) return TAL_ECUDA;
     int flags = 0;
     e = cudaMemcpyAsync(&flags, &c->flags, sizeof(flags), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return TAL_ECUDA;
-    return flags ? TAL_EDOMAIN : TAL_OK;
+    // a pair whose rows do not fit shared memory: a capacity refusal; a pair
+    // outside the exact range or with a base code above 4: a domain error
+    if (flags & (talbsw::ERR_DOMAIN | talbsw::ERR_BASE)) return TAL_EDOMAIN;
+    if (flags) return TAL_ENOMEM;
+    return TAL_OK;
 }

@@ -143,6 +143,7 @@ struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     DevBuf counts, order, order_req, seg, ctrl, dreqs;
+    RegroupBufs rg;  // exact scoring of the tick's flagged pairs' SIMD groups
     BinFork fork;
     ReqDesc *hreqs = nullptr;  // pinned copy of the tick's request table
     std::vector<Request *> reqs;
@@ -320,6 +321,7 @@ int tal_bsw_server::launch_tick(Slot &sl) {
     LaunchArgs base;
     memset(&base, 0, sizeof(base));
     base.reqs = dreqs;
+    attach_regroup(base, sl.rg.V);  // the scoring launches flag pairs for the regroup pass
     if (e == cudaSuccess && total > 0) e = enqueue_sort(h, sb, base, nreq, (int)total, sl.stream);
     // a small tick cannot hide a lane walking a long pair behind other work:
     // a handful of launches, pairs above 256 columns with G lanes each; a
@@ -329,6 +331,15 @@ int tal_bsw_server::launch_tick(Slot &sl) {
             e = enqueue_tick(h, sb, base, segs, 7, sl.fork, sl.stream);
         else
             e = enqueue_segs_forked(h, sb, base, segs, (int)total, 100, sl.fork, sl.stream, false);
+    }
+    // the SIMD groups of flagged pairs, per request (errors into its table entry)
+    if (e == cudaSuccess && total > 0) {
+        LaunchArgs rg = base;
+        rg.err_flags = &sb.ctrl->flags;
+        rg.err_index = &sb.ctrl->bad_index;
+        rg.cells = &sb.ctrl->cells;
+        rg.P = h->kp;
+        e = enqueue_regroup(sl.rg.V, rg, nreq, total, h->num_sms, sl.stream, nullptr);
     }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(sl.hreqs, dreqs, sizeof(ReqDesc) * nreq, cudaMemcpyDeviceToHost, sl.stream);
@@ -453,6 +464,7 @@ void free_server(tal_bsw_server *s) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         sl.counts.release(); sl.order.release(); sl.order_req.release();
         sl.seg.release(); sl.ctrl.release(); sl.dreqs.release();
+        sl.rg.release();
         if (sl.hreqs) cudaFreeHost(sl.hreqs);
         sl.fork.release();
         if (sl.done) cudaEventDestroy(sl.done);
@@ -534,6 +546,8 @@ int tal_bsw_server_create(tal_bsw_handle src, const tal_bsw_server_config *cfg,
         if (e == cudaSuccess) e = sl.seg.ensure(sizeof(int32_t) * 2 * kNumSegs);
         if (e == cudaSuccess) e = sl.ctrl.ensure(sizeof(BatchCtrl));
         if (e == cudaSuccess) e = sl.dreqs.ensure(sizeof(ReqDesc) * kMaxTickRequests);
+        bool grown = false;
+        if (e == cudaSuccess) e = sl.rg.ensure(c.max_tick_pairs, 32767, s->h->num_sms, &grown);
         if (e == cudaSuccess) e = sl.fork.create();
         if (e == cudaSuccess)
             e = cudaHostAlloc(reinterpret_cast<void **>(&sl.hreqs), sizeof(ReqDesc) * kMaxTickRequests,
@@ -594,6 +608,9 @@ int tal_bsw_submit(tal_bsw_server_handle s, tal_seq_pair *pairs, const uint8_t *
     bool done_now = numPairs == 0 || bad >= 0;
     if (!done_now) {
         rlo &= ~15LL;
+        // the padding lanes of a request's last partial 8-bit group, when its
+        // SIMD groups are re-scored exactly, read the query at offset 0
+        if (bits != 16 && qlo <= (1 << 20)) qlo = 0;
         qlo &= ~15LL;
         if (rhi <= rlo) rhi = rlo + 16;
         if (qhi <= qlo) qhi = qlo + 16;

@@ -55,6 +55,8 @@ _SIGS = {
     "tal_bsw_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
     "tal_bsw_last_kernel_ms": (ctypes.c_float, [ctypes.c_void_p]),
     "tal_bsw_last_cells": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "tal_bsw_last_regroup": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                            ctypes.POINTER(ctypes.c_int64)]),
     "tal_bsw_scores_batched_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                      ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
                                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
@@ -202,6 +204,7 @@ class BandedPairWiseSW:
             wp = wpair.ctypes.data
         self._check(self._lib.tal_bsw_scores_batched(self._h, pa.ctypes.data, _buf_ptr(seqBufRef),
                                                      _buf_ptr(seqBufQer), n, int(w), wp, int(bits)))
+        self.SW_cells += self.last_cells
 
     def scores_batched_device(self, d_pairs: int, d_ref: int, ref_bytes: int, d_qer: int,
                               qer_bytes: int, numPairs: int, w: int, bits: int = AUTO,
@@ -248,6 +251,14 @@ class BandedPairWiseSW:
         """DP cells computed by the last collected call."""
         return int(self._lib.tal_bsw_last_cells(self._h))
 
+    def last_regroup(self):
+        """(pairs flagged, SIMD groups re-scored) by the last collected call:
+        the pairs whose outputs could depend on their group in the reference,
+        and the groups scored again with the reference's grouping for them."""
+        f, g = ctypes.c_int64(0), ctypes.c_int64(0)
+        self._check(self._lib.tal_bsw_last_regroup(self._h, ctypes.byref(f), ctypes.byref(g)))
+        return int(f.value), int(g.value)
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._lib.tal_bsw_destroy(self._h)
@@ -280,6 +291,9 @@ class BandedPairWiseSW:
         rc = self._lib.tal_bsw_scores(self._h, pa.ctypes.data, _buf_ptr(seqBufRef),
                                       _buf_ptr(seqBufQer), n, int(w), int(bits))
         self._check(rc)
+        # the reference's counter of DP cells (bandedSWA.h:116, never
+        # incremented there): kept here from the library's own count
+        self.SW_cells += self.last_cells
 
 
 def now_ns() -> int:
