@@ -17,7 +17,7 @@ def build(force=False):
     srcs = [os.path.join(HERE, "emu.cpp"), os.path.join(HERE, "fake", "cuda_runtime.h"),
             os.path.join(CSRC, "bsw_kernel.cuh"), os.path.join(CSRC, "bsw_lane.cuh"),
             os.path.join(CSRC, "sw_kernel.cuh"), os.path.join(CSRC, "bsw_group.cuh"),
-            os.path.join(CSRC, "bsw_couple.cuh")]
+            os.path.join(CSRC, "bsw_couple.cuh"), os.path.join(CSRC, "bsw_group_wide.cuh")]
     if force or not os.path.exists(SO) or os.path.getmtime(SO) < max(os.path.getmtime(s) for s in srcs):
         os.makedirs(os.path.dirname(SO), exist_ok=True)
         subprocess.check_call(["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-pthread", "-w",
@@ -99,6 +99,49 @@ def run_group(pairs, ref, qer, w, params, bits=16, warps=2, ref_lo=0, qer_lo=0):
                                 ctypes.byref(ef), ctypes.byref(ei))
     assert rc == 0, "divergent warp exit"
     return out, ef.value, ei.value
+
+
+def run_group_wide(pairs, ref, qer, w, params, bits=16, smem_rows=1 << 20, groups=None,
+                   ref_lo=0, qer_lo=0):
+    """Scores a copy of pairs with the emulated block-wide grouped kernel.
+    groups=None: the reference's groups of consecutive pairs, every lane
+    wanted.  groups = [(members, need_mask)]: member mode, members a list of
+    pair indices (-1: padding lane) of one group, need_mask the lanes whose
+    outputs are written.  smem_rows: shared memory for the group's rows (0:
+    the global slot).  Returns (pairs, err_flags, err_index, cells)."""
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+    out = np.ascontiguousarray(pairs).copy()
+    kp = np.array([params[k] for k in ("o_del", "e_del", "o_ins", "e_ins", "zdrop", "end_bonus", "a", "b")],
+                  np.int32)
+    ef = ctypes.c_int(0)
+    ei = ctypes.c_longlong(0)
+    cells = ctypes.c_ulonglong(0)
+    ref = np.ascontiguousarray(ref)
+    qer = np.ascontiguousarray(qer)
+    vp = ctypes.c_void_p
+    mem = gin = need = None
+    ng = 0
+    if groups is not None:
+        ng = len(groups)
+        mem = np.full((max(ng, 1), 64), -1, np.int64)
+        gin = np.zeros((max(ng, 1), 4), np.int32)
+        need = np.zeros(max(ng, 1), np.uint64)
+        for g, (members, mask) in enumerate(groups):
+            mem[g, :len(members)] = members
+            real = [m for m in members if m >= 0]
+            gin[g] = (w, -1, int(pairs["len2"][real[-1]]) if real else 0, 0)
+            need[g] = np.uint64(mask)
+    rc = _lib.emu_bsw_group_wide_run(
+        vp(out.ctypes.data), vp(ref.ctypes.data), ctypes.c_longlong(ref_lo),
+        ctypes.c_longlong(ref_lo + ref.shape[0]), vp(qer.ctypes.data), ctypes.c_longlong(qer_lo),
+        ctypes.c_longlong(qer_lo + qer.shape[0]), int(out.shape[0]), int(w), int(bits), vp(kp.ctypes.data),
+        None if mem is None else vp(mem.ctypes.data), None if gin is None else vp(gin.ctypes.data),
+        None if need is None else vp(need.ctypes.data), int(ng), ctypes.c_longlong(smem_rows),
+        ctypes.byref(ef), ctypes.byref(ei), ctypes.byref(cells))
+    assert rc == 0, "divergent warp"
+    return out, ef.value, ei.value, cells.value
 
 
 def run_reqs(reqs, order, params, K=4, warps=1, G=32, win=0):

@@ -22,6 +22,7 @@ std::mutex atomic_mu;
 #include "sw_kernel.cuh"
 #include "chain_kernel.cuh"
 #include "bsw_group.cuh"
+#include "bsw_group_wide.cuh"
 #include <functional>
 
 // Runs one launch of A (one block of `warps` warps); -1 if a warp's lanes
@@ -173,6 +174,116 @@ extern "C" int emu_bsw_group_run(talbsw::DevPair *pairs, const uint8_t *ref, lon
     const int rc = run_launch(A, 1, 4, warps);
     g_group = nullptr;
     return rc;
+}
+
+// One block of `warps` warps running body() in every lane, the warps
+// interleaved so that __syncthreads() holds: a warp whose lanes all wait at
+// the block barrier is skipped until every warp still running waits there.
+// -1 on a divergent warp (its lanes at different barriers or exits).
+static int run_block(void (*body)(const void *), const void *arg, int warps, unsigned char *smem) {
+    std::vector<simt::Warp *> Ws(warps);
+    std::vector<std::vector<char>> stacks((size_t)32 * warps, std::vector<char>(1 << 18));
+    struct BArg { int t; simt::Warp *W; unsigned char *sm; int warps; void (*body)(const void *); const void *arg; };
+    static thread_local std::vector<BArg> bargs;
+    bargs.assign((size_t)32 * warps, BArg{});
+    for (int wi = 0; wi < warps; wi++) {
+        Ws[wi] = new simt::Warp();
+        for (int l = 0; l < 32; l++) {
+            const int t = wi * 32 + l;
+            bargs[t] = BArg{t, Ws[wi], smem, warps, body, arg};
+            getcontext(&Ws[wi]->lane_ctx[l]);
+            Ws[wi]->lane_ctx[l].uc_stack.ss_sp = stacks[t].data();
+            Ws[wi]->lane_ctx[l].uc_stack.ss_size = stacks[t].size();
+            Ws[wi]->lane_ctx[l].uc_link = &Ws[wi]->sched;
+            makecontext(&Ws[wi]->lane_ctx[l], (void (*)())+[](int t2) {
+                BArg &a = bargs[t2];
+                simt::tl_threadIdx.x = a.t;
+                simt::tl_blockIdx.x = 0;
+                simt::tl_blockDim.x = 32 * a.warps;
+                simt::tl_gridDim.x = 1;
+                simt::tl_warp = a.W;
+                simt::tl_smem = a.sm;
+                a.body(a.arg);
+                a.W->done[a.t & 31] = true;
+            }, 1, t);
+        }
+    }
+    int divergent = 0;
+    for (;;) {
+        bool ran = false, live = false;
+        for (int wi = 0; wi < warps && !divergent; wi++) {
+            simt::Warp *W = Ws[wi];
+            int nlive = 0, nbar = 0;
+            for (int l = 0; l < 32; l++) {
+                if (W->done[l]) continue;
+                nlive++;
+                nbar += W->at_bar[l];
+            }
+            if (nlive == 0) continue;
+            live = true;
+            if (nbar == nlive) continue;  // waiting at the block barrier
+            if (nbar != 0 || nlive != 32) { divergent = 1; break; }
+            for (int l = 0; l < 32; l++) {
+                simt::tl_warp = W;
+                simt::tl_threadIdx.x = wi * 32 + l;
+                simt::tl_smem = smem;
+                swapcontext(&W->sched, &W->lane_ctx[l]);
+            }
+            ran = true;
+        }
+        if (divergent || !live) break;
+        if (!ran)  // every running warp waits at the barrier: release it
+            for (int wi = 0; wi < warps; wi++)
+                for (int l = 0; l < 32; l++) Ws[wi]->at_bar[l] = false;
+    }
+    for (int wi = 0; wi < warps; wi++) delete Ws[wi];
+    return divergent ? -1 : 0;
+}
+
+// The block-wide grouped kernel (bsw_group_wide.cuh) over n pairs with one
+// band, one block taking every group; smem_rows: shared-memory bytes for the
+// group's rows (0: every group uses the global slot).  members / ginfo /
+// need / ngroups: member mode (null members: consecutive groups of n).
+extern "C" int emu_bsw_group_wide_run(talbsw::DevPair *pairs, const uint8_t *ref, long long ref_lo,
+                                      long long ref_hi, const uint8_t *qer, long long qer_lo,
+                                      long long qer_hi, int n, int w, int bits, const int32_t *kp,
+                                      const long long *members, const int *ginfo,
+                                      const unsigned long long *need, int ngroups,
+                                      long long smem_rows, int *err_flags, long long *err_index,
+                                      unsigned long long *cells) {
+    talbsw::GroupArgs G;
+    std::memset(&G, 0, sizeof(G));
+    G.pairs = pairs;
+    G.ref = ref; G.ref_lo = ref_lo; G.ref_hi = ref_hi;
+    G.qer = qer; G.qer_lo = qer_lo; G.qer_hi = qer_hi;
+    G.n = n; G.w = w; G.bits = bits;
+    int m2 = 1;
+    for (int i = 0; i < n; i++) m2 = std::max(m2, pairs[i].len2);
+    G.col_cap = m2 + 3;
+    G.slot_elems = talbsw::group_slot_elems(G.col_cap, bits);
+    std::vector<int16_t> scratch(G.slot_elems, (int16_t)0x5a5a);  // poisoned
+    G.scratch = scratch.data();
+    int counter = 0, ng = ngroups;
+    *cells = 0;
+    *err_flags = 0; *err_index = (long long)INT64_MAX;
+    G.work_counter = &counter; G.cells = cells; G.err_flags = err_flags; G.err_index = err_index;
+    G.P = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], kp[6], kp[7]};
+    G.ngroups_cap = 1 << 30;
+    if (members) {
+        G.members = members;
+        G.ginfo = reinterpret_cast<const int4 *>(ginfo);
+        G.need = need;
+        G.ngroups_dev = &ng;
+    }
+    const size_t xb = talbsw::wide_x_bytes<talbsw::kWideWarps>();
+    G.smem_bytes = xb + (size_t)smem_rows;
+    std::vector<unsigned char> smem(G.smem_bytes + 64, 0xA5);  // poisoned, like fresh smem
+    auto body = [](const void *a) {
+        const talbsw::GroupArgs &g = *static_cast<const talbsw::GroupArgs *>(a);
+        if (g.bits == 8) talbsw::group_wide_body<8, talbsw::kWideWarps>(g, simt::tl_smem);
+        else talbsw::group_wide_body<16, talbsw::kWideWarps>(g, simt::tl_smem);
+    };
+    return run_block(body, &G, talbsw::kWideWarps, smem.data());
 }
 
 // A serving tick: nreq requests, each with its own pair array, sequence

@@ -36,6 +36,7 @@ struct Warp {
     int64_t slot[2][32];
     int phase[32] = {0};
     bool done[32] = {false};
+    bool at_bar[32] = {false};  // waiting at a block barrier (multi-warp blocks)
     void barrier(int l) { swapcontext(&lane_ctx[l], &sched); }
 };
 struct Dim { unsigned x = 0, y = 0, z = 0; };
@@ -138,9 +139,15 @@ inline int __reduce_min_sync(unsigned, int v) {
     return r;
 }
 inline void __syncwarp(unsigned = 0xffffffffu) { simt::tl_warp->barrier(simt::lane()); }
-// Block barriers appear only in kernels the emulator never runs (the work
-// order sort); warps here run one after another, so none could be honoured.
-inline void __syncthreads() { std::abort(); }
+// A block barrier: the lane waits until every warp of the block has
+// arrived (emu.cpp's block scheduler releases them); a one-warp launch
+// treats it as a warp barrier.
+inline void __syncthreads() {
+    simt::Warp *w = simt::tl_warp;
+    const int l = simt::lane();
+    w->at_bar[l] = true;
+    w->barrier(l);
+}
 inline unsigned __umulhi(unsigned a, unsigned b) { return (unsigned)(((unsigned long long)a * b) >> 32); }
 inline int __ffs(unsigned x) { return x ? __builtin_ctz(x) + 1 : 0; }
 inline int __clz(unsigned x) { return x ? __builtin_clz(x) : 32; }

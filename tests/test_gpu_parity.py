@@ -412,3 +412,27 @@ def test_per_pair_equals_grouped_on_workloads(wl, n):
                 bsw._scores(a, b.ref, b.qer, a.shape[0], int(wv), bits)
                 bsw._scores(g, b.ref, b.qer, g.shape[0], int(wv), bits | GROUPED)
                 _assert_same(g, a, f"{wl.name} w={wv} bits={bits}: per pair vs grouped")
+
+
+def test_scalar_wrapper_matches_the_scalar_path():
+    """scalarBandedSWAWrapper / scalarBandedSWA (bandedSWA.cpp:116-260) run on
+    the GPU with every pair alone in its group: equal to the oracle's port of
+    the reference's scalar code at e_del = e_ins = 1; other gap extensions
+    are refused."""
+    b = synth.generate(synth.C2.scaled(2000, seed=31))
+    P = b.workload.params()
+    exp, _ = oracle.scalar(b.pairs, b.ref, b.qer, 100, P)
+    with _bsw(P) as bsw:
+        got = b.pairs.copy()
+        bsw.scalarBandedSWAWrapper(got, b.ref, b.qer, b.n, 1, 100)
+        _assert_same(exp, got, "scalarBandedSWAWrapper")
+        p0 = b.pairs[7]
+        q = b.qer[p0["idq"]:p0["idq"] + p0["len2"]]
+        t = b.ref[p0["idr"]:p0["idr"] + p0["len1"]]
+        r = bsw.scalarBandedSWA(int(p0["len2"]), q, int(p0["len1"]), t, 100, int(p0["h0"]))
+        e = exp[7]
+        assert r == (e["score"], e["qle"], e["tle"], e["gtle"], e["gscore"], e["max_off"])
+    P2 = dict(P, e_del=2, e_ins=2)
+    with _bsw(P2) as bsw:
+        with pytest.raises(tal_bsw.TalBswError):
+            bsw.scalarBandedSWAWrapper(b.pairs.copy(), b.ref, b.qer, b.n, 1, 100)

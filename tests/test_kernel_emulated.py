@@ -347,6 +347,59 @@ def test_emulated_group_kernel_matches_golden(f):
     assert bad.size == 0, f"pair {bad[0]}: emu {g[bad[0]].tolist()} ref {e[bad[0]].tolist()}"
 
 
+@pytest.mark.parametrize("f", GROUPED_FILES, ids=os.path.basename)
+def test_emulated_wide_group_kernel_matches_golden(f):
+    """The block-wide grouped kernel (bsw_group_wide.cuh: four warps share a
+    group's columns, E carried across their chunks) gives the reference's
+    outputs, with the group's rows in shared memory and, on a few fixtures,
+    in the global slot."""
+    d = np.load(f)
+    P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+    bits = int(d["bits"])
+    lanes = 64 if bits == 8 else 32
+    n = d["inputs"].shape[0] if "coupled" in f else min(d["inputs"].shape[0], 3 * lanes + 5)
+    p = d["inputs"][:n]
+    exp = d["expected"][:n] if n == d["inputs"].shape[0] else oracle.vector(p, d["ref"], d["qer"], int(d["w"]), P, bits=bits)
+    name = os.path.basename(f)
+    for rows in ((1 << 20, 0) if name in ("coupled16_band_4.npz", "wrap8_gap_open_130_band_5.npz",
+                                         "edge16_band_3.npz") else (1 << 20,)):
+        got, ef, _, _ = simt_emu.run_group_wide(p, d["ref"], d["qer"], int(d["w"]), P, bits=bits, smem_rows=rows)
+        assert ef == 0
+        e, g = outputs(exp), outputs(got)
+        bad = np.nonzero((e != g).any(1))[0]
+        assert bad.size == 0, f"rows {rows}: pair {bad[0]}: emu {g[bad[0]].tolist()} ref {e[bad[0]].tolist()}"
+
+
+@pytest.mark.parametrize("f", COUPLED + [os.path.join(GOLDEN, "wrap8_gap_open_130_band_5.npz"),
+                                         os.path.join(GOLDEN, "edge16_zdrop_1.npz")], ids=os.path.basename)
+def test_emulated_wide_group_kernel_member_mode(f):
+    """Member mode (the regroup pass): groups given as member lists with the
+    lanes whose outputs are wanted; those lanes get the reference's outputs
+    (the group stops once they have exited), every other pair is untouched."""
+    d = np.load(f)
+    P = {k: int(v) for k, v in zip(d["param_keys"], d["param_vals"])}
+    bits = int(d["bits"])
+    lanes = 64 if bits == 8 else 32
+    p = d["inputs"][:3 * lanes + 7]
+    n = p.shape[0]
+    w = int(d["w"])
+    exp = oracle.vector(p, d["ref"], d["qer"], w, P, bits=bits)
+    rng = np.random.default_rng(7)
+    groups, wanted = [], np.zeros(n, bool)
+    for g in range(0, n, lanes):
+        members = list(range(g, min(g + lanes, n)))
+        k = len(members)
+        mask = 0
+        for l in rng.choice(k, size=min(k, 1 + g // lanes), replace=False):
+            mask |= 1 << int(l)
+            wanted[g + int(l)] = True
+        groups.append((members + [-1] * (lanes - k), mask))
+    got, ef, _, _ = simt_emu.run_group_wide(p, d["ref"], d["qer"], w, P, bits=bits, groups=groups[::-1])
+    assert ef == 0
+    assert (outputs(got)[wanted] == outputs(exp)[wanted]).all()
+    assert (outputs(got)[~wanted] == outputs(p)[~wanted]).all()
+
+
 @pytest.mark.parametrize("f", COUPLED, ids=os.path.basename)
 def test_emulated_lane_kernel_on_coupled_fixtures_scores_pairs_alone(f):
     """On the fixtures where the grouping matters, the per-pair lane kernel

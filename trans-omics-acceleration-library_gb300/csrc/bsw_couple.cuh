@@ -90,27 +90,23 @@ struct Couple {
     }
     // the checks that need only the row's scalars, before its cells
     // (active: the lane is still scoring this row; h10init: the row's
-    // column-(beg - 1) value, hv_next: H_v[i + 1]); cmax = element limit
+    // column-(beg - 1) value, hv_next: H_v[i + 1]); cmax = element limit.
+    // Straight-line selects: the lanes of a warp hold different pairs.
     __device__ void row_checks(bool was_active, bool mlen_exit, bool active, int i, int w,
-                                        int beg, int end, int len2, int h10init,
-                                        int hv_next, int cmax) {
-        if (was_active && !mlen_exit && tlo <= hhi && thi > hlo) flag |= CPL_EXIT;
-        if (!active) return;
+                               int beg, int end, int len2, int h10init, int hv_next, int cmax) {
+        int f = 0;
+        f |= (was_active && !mlen_exit && tlo <= hhi && thi > hlo) ? CPL_EXIT : 0;
         const bool uncH = hlo != hhi;
-        if (tlo != thi) flag |= CPL_TAIL;
-        if (uncH && hhi > end) flag |= CPL_HEAD;
-        if (uncH && beg >= hlo && beg < hhi && h10init != 0) flag |= CPL_HEAD;
+        f |= (active && tlo != thi) ? CPL_TAIL : 0;
+        f |= (active && uncH && (hhi > end || (beg >= hlo && beg < hhi && h10init != 0))) ? CPL_HEAD : 0;
         const int lo = imax(0, i - w);
-        if (beg > lo) {
-            if (fzMax >= lo) flag |= CPL_LEFT;
-            else if (lo == 0 && hlo <= 0 && hv_next != 0) flag |= CPL_LEFT;  // H_v[i + 1] at column 0
-        }
+        const bool left = beg > lo && (fzMax >= lo || (lo == 0 && hlo <= 0 && hv_next != 0));  // H_v[i + 1] at column 0
+        f |= (active && left) ? CPL_LEFT : 0;
         const int Emax = imin(i + w + 1, cmax);
-        if (end < Emax) {
-            if (end < thi) flag |= CPL_RIGHT;
-            const int c0 = imax(imax(end, tlo), maxEnd) + 1;
-            if (c0 <= imin(Emax, len2 - 1) && c0 < K0) flag |= CPL_STALE;
-        }
+        const int c0 = imax(imax(end, tlo), maxEnd) + 1;
+        f |= (active && end < Emax && end < thi) ? CPL_RIGHT : 0;
+        f |= (active && end < Emax && c0 <= imin(Emax, len2 - 1) && c0 < K0) ? CPL_STALE : 0;
+        flag |= f;
     }
     // the range [beg, trim_hi) whose old entries must be zero when the lane
     // does not trim the row or its head is uncertain (empty: beg >= trim_hi)
@@ -147,48 +143,51 @@ struct Couple {
     // everything this lane wrote; -1 if none
     __device__ int first_right_nz(int a, int b, int len2, int cmax) const {
         const int c0 = imax(a, maxEnd) + 1;
-        if (c0 <= b && c0 < len2 && c0 < K0) return c0;
-        if (len2 > a && len2 <= b && (Fv > 0 || (!reached && len2 < K0))) return len2;
         const int c1 = imax(a, len2) + 1;
-        if (c1 <= b && c1 < cmax && c1 < K0) return c1;
-        return -1;
+        const bool own = c0 <= b && c0 < len2 && c0 < K0;
+        const bool atq = len2 > a && len2 <= b && (Fv > 0 || (!reached && len2 < K0));
+        const bool past = c1 <= b && c1 < cmax && c1 < K0;
+        return own ? c0 : atq ? len2 : past ? c1 : -1;
     }
     // the head / tail scans' results (bandedSWA.cpp:3265-3316): sb / se their
     // ranges, nz_sb / nz_se whether the lane is non-zero there, newhead /
     // index the lane's own results, run_end / run_bot whether its runs
-    // reached the range's end; last_row: no row of this lane follows
+    // reached the range's end; last_row: no row of this lane follows.
+    // Straight-line selects, as row_checks.
     __device__ void scans(bool ex, bool last_row, bool is8, int i, int w, int beg, int end,
-                                   int sb, int se, bool nz_sb, bool nz_se, bool run_end,
-                                   bool hse_nz, bool run_bot, int newhead, int index, int qlenE,
-                                   int len2, int cmax) {
-        if (ex && !last_row) {
-            if (run_end && !(se <= end && hse_nz)) flag |= CPL_RUNEND;
-            if (run_bot) flag |= CPL_RUNBOT;
-            const int lo = imax(0, i - w);
-            const int los = is8 ? lo : 0;
-            int nhlo, nhhi;
-            if (nz_sb) { nhlo = hlo; nhhi = hhi; } else { nhlo = nhhi = newhead; }
-            if (sb > los) {
-                int Pl = -1;
-                if (!is8) { if (fzMin < sb) Pl = imin(fzMax, sb - 1); }
-                else if (fzMax >= lo) Pl = fzMax;
-                if (nz_sb && Pl < sb - 1) { nhlo = imin(nhlo, sb); nhhi = imax(nhhi, sb); }
-                if (Pl >= 0) { nhlo = imin(imin(nhlo, hlo), los); nhhi = imax(imax(nhhi, hhi), Pl); }
-            }
-            const int Emax = imin(i + w + 1, cmax);
-            const int Smax = is8 ? Emax : imin(Emax + 2, cmax);
-            int rlo, rhi;
-            if (nz_se) { rlo = tlo; rhi = thi; } else { rlo = rhi = index; }
-            if (Smax > se) {
-                const int Qr = first_right_nz(imax(se, end), Smax, len2, cmax);
-                if (nz_se) { rlo = imin(rlo, se); rhi = imax(rhi, se); }
-                if (Qr >= 0) { rlo = imin(imin(rlo, tlo), Qr); rhi = imax(imax(rhi, thi), Smax - 1); }
-            }
-            tlo = imin(rlo + 2, qlenE);
-            thi = imin(rhi + 2, qlenE);
-            hlo = nhlo;
-            hhi = nhhi;
-        }
+                          int sb, int se, bool nz_sb, bool nz_se, bool run_end, bool hse_nz,
+                          bool run_bot, int newhead, int index, int qlenE, int len2, int cmax) {
+        const bool go = ex && !last_row;
+        int f = (run_end && !(se <= end && hse_nz)) ? CPL_RUNEND : 0;
+        f |= run_bot ? CPL_RUNBOT : 0;
+        flag |= go ? f : 0;
+        const int lo = imax(0, i - w);
+        const int los = is8 ? lo : 0;
+        int nhlo = nz_sb ? hlo : newhead, nhhi = nz_sb ? hhi : newhead;
+        const int Pl16 = fzMin < sb ? imin(fzMax, sb - 1) : -1;
+        const int Pl8 = fzMax >= lo ? fzMax : -1;
+        const int Pl = sb > los ? (is8 ? Pl8 : Pl16) : -1;
+        const bool c1 = sb > los && nz_sb && Pl < sb - 1;
+        nhlo = c1 ? imin(nhlo, sb) : nhlo;
+        nhhi = c1 ? imax(nhhi, sb) : nhhi;
+        const bool c2 = Pl >= 0;
+        nhlo = c2 ? imin(imin(nhlo, hlo), los) : nhlo;
+        nhhi = c2 ? imax(imax(nhhi, hhi), Pl) : nhhi;
+        const int Emax = imin(i + w + 1, cmax);
+        const int Smax = is8 ? Emax : imin(Emax + 2, cmax);
+        int rlo = nz_se ? tlo : index, rhi = nz_se ? thi : index;
+        const bool c3 = Smax > se;
+        const int Qr = c3 ? first_right_nz(imax(se, end), Smax, len2, cmax) : -1;
+        const bool c4 = c3 && nz_se;
+        rlo = c4 ? imin(rlo, se) : rlo;
+        rhi = c4 ? imax(rhi, se) : rhi;
+        const bool c5 = Qr >= 0;
+        rlo = c5 ? imin(imin(rlo, tlo), Qr) : rlo;
+        rhi = c5 ? imax(imax(rhi, thi), Smax - 1) : rhi;
+        tlo = go ? imin(rlo + 2, qlenE) : tlo;
+        thi = go ? imin(rhi + 2, qlenE) : thi;
+        hlo = go ? nhlo : hlo;
+        hhi = go ? nhhi : hhi;
     }
     // keeps the lane's own head / tail inside the intervals (after a row)
     __device__ void settle(bool ex, bool last_row, int head, int tail) {

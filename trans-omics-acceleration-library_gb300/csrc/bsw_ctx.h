@@ -133,12 +133,14 @@ struct RegroupView {
     int4 *cinfo = nullptr;
     int *counts = nullptr, *offsets = nullptr, *totals = nullptr;
     unsigned long long *mhash = nullptr;
+    unsigned long long *needh = nullptr;  // per hash slot: the flagged lanes of its group
+    unsigned long long *gneed = nullptr;  // per marked group: the same, in list order
     int2 *mlist = nullptr;
     int *mslot = nullptr;
     long long *members = nullptr;
     int4 *ginfo = nullptr;
     int16_t *scratch = nullptr;
-    int nchunks = 0, fcap = 0, mcap = 0, hcap = 0, col_cap = 0, warps = 0;
+    int nchunks = 0, fcap = 0, mcap = 0, hcap = 0, col_cap = 0, slots = 0, smem = 0;
 };
 struct RegroupBufs {
     DevBuf arena;

@@ -41,7 +41,8 @@ struct GroupArgs {
     int *err_flags;
     long long *err_index;
     KernelParams P;
-    // member mode (re-scoring the groups of flagged pairs, bsw_regroup.cu):
+    // member mode (the block-wide kernel of the regroup pass, bsw_regroup.cu,
+    // bsw_group_wide.cuh; the one-warp kernel here scores consecutive groups):
     // group g's lane l is the pair with global index members[g * 64 + l]
     // (-1: a padding lane), its band and request are ginfo[g] {w, req,
     // padding lanes' len2, -}, and the groups are 0 .. *ngroups_dev; a
@@ -53,6 +54,9 @@ struct GroupArgs {
     int ngroups_cap = 1 << 30;
     ReqDesc *reqs = nullptr;
     int nreq = 0;
+    const unsigned long long *need = nullptr;  // per group, the lanes whose outputs are
+                                               // wanted (bit l: lane l; null: all)
+    size_t smem_bytes = 0;  // the block-wide kernel's dynamic shared memory per block
 };
 
 // Global pair index -> (request, local index) in a serving tick's pair space.
@@ -76,6 +80,13 @@ __host__ __device__ inline size_t group_slot_elems(int col_cap, int bits) {
     const size_t l = (size_t)group_lanes(bits);
     const size_t qbytes = ((((size_t)col_cap + 3) & ~(size_t)3) + 8) * l;  // + two words read ahead
     return ((size_t)col_cap * l * 2 + (qbytes + 1) / 2 + 8 + 7) & ~(size_t)7;
+}
+
+// Bytes of a group's rows held in shared memory (block-wide kernel): the
+// (H, F) words of col_cap columns and the query codes, as in a scratch slot.
+__host__ __device__ inline size_t group_smem_bytes(int col_cap, int bits) {
+    const size_t l = (size_t)group_lanes(bits);
+    return (size_t)col_cap * l * 4 + ((((size_t)col_cap + 3) & ~(size_t)3) + 8) * l + 16;
 }
 
 __host__ __device__ __forceinline__ unsigned umin(unsigned a, unsigned b) { return a < b ? a : b; }
@@ -104,8 +115,7 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
     uint32_t *HF = reinterpret_cast<uint32_t *>(A.scratch + (size_t)gw * A.slot_elems);
     int8_t *Q2 = reinterpret_cast<int8_t *>(HF + (size_t)A.col_cap * W);
     const KernelParams &P = A.P;
-    const bool mm = A.members != nullptr;  // member mode
-    const int ngroups = mm ? imin(*A.ngroups_dev, A.ngroups_cap) : (A.n + W - 1) / W;
+    const int ngroups = (A.n + W - 1) / W;
 
     // scores and constants (bandedSWA.cpp:50-68), wrapped to the element width
     const int w_match = E::ws((int8_t)P.a);
@@ -133,41 +143,18 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
         long long lidx[LPT];  // the pair's index in its caller's array (for errors)
         bool real[LPT];
         bool bad = false;
-        // this group's band, sequence windows and request
-        int gw = A.w, greq = -1, padq = 0;
-        DevPair *gpairs = A.pairs;
+        const int gw = A.w;
         const uint8_t *Aref = A.ref, *Aqer = A.qer;
-        long long ref_lo = A.ref_lo, ref_hi = A.ref_hi, qer_lo = A.qer_lo, qer_hi = A.qer_hi;
-        if (mm) {
-            const int4 gi = A.ginfo[g];
-            gw = gi.x; greq = gi.y; padq = gi.z;
-            if (greq >= 0) {
-                const ReqDesc &d = A.reqs[greq];
-                gpairs = d.pairs;
-                Aref = d.ref; Aqer = d.qer;
-                ref_lo = d.ref_lo; ref_hi = d.ref_hi; qer_lo = d.qer_lo; qer_hi = d.qer_hi;
-            }
-        }
+        const long long ref_lo = A.ref_lo, ref_hi = A.ref_hi, qer_lo = A.qer_lo, qer_hi = A.qer_hi;
         auto gerr = [&](int flag, long long k) {
             atomicOr(A.err_flags, flag);
-            if (greq >= 0) {
-                atomicOr(&A.reqs[greq].err, flag);
-                atomicMin(&A.reqs[greq].bad, k);
-            } else {
-                atomicMin(A.err_index, k);
-            }
+            atomicMin(A.err_index, k);
         };
         for (int u = 0; u < LPT; u++) {
-            long long k = (long long)g * W + t + 32 * u;
-            if (mm) {
-                k = A.members[(size_t)g * 64 + t + 32 * u];
-                real[u] = k >= 0;
-                if (real[u] && greq >= 0) k -= A.reqs[greq].first;
-            } else {
-                real[u] = k < A.n;
-            }
+            const long long k = (long long)g * W + t + 32 * u;
+            real[u] = k < A.n;
             lidx[u] = k;
-            pp[u] = real[u] ? gpairs + k : nullptr;
+            pp[u] = real[u] ? A.pairs + k : nullptr;
             if (real[u]) {
                 const DevPair &p = *pp[u];
                 len1[u] = p.len1; len2[u] = p.len2; h0r[u] = p.h0;
@@ -183,7 +170,7 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
                 }
             } else {
                 len1[u] = 0;
-                len2[u] = is16 ? 0 : (mm ? padq : A.pairs[A.n - 1].len2);
+                len2[u] = is16 ? 0 : A.pairs[A.n - 1].len2;
                 h0r[u] = 0;
                 idr[u] = idq[u] = -1;
             }

@@ -486,6 +486,38 @@ __device__ __forceinline__ int scan_last_nz(const int *Hh, const int *Fv, int lo
 
 namespace talbsw {
 
+// One pass over [a, c) for the coupling detector: the lowest and highest
+// non-zero column of [a, b) (columns freezing this row) and whether [b, c)
+// (old entries a group may trim) holds a non-zero.  Warp-uniform loop; each
+// pair searches with its own G lanes, G columns per ballot.
+template <int G>
+__device__ __forceinline__ void scan_frozen_trim(const int *Hh, const int *Fv, int a, int b, int c,
+                                                 bool act, int gl, int gshift, unsigned gbits, int wm,
+                                                 int &fmin, int &fmax, bool &tnz) {
+    fmin = 1 << 30;
+    fmax = -1;
+    tnz = false;
+    bool srch = act && a < c;
+    int base = a;
+    while (__any_sync(0xffffffffu, srch)) {
+        const int j = base + gl;
+        const bool nz = srch && j < c && ((Hh[j & wm] | Fv[j & wm]) != 0);
+        const unsigned m = (__ballot_sync(0xffffffffu, nz) & gbits) >> gshift;  // bit k: column base + k
+        if (srch) {
+            const int nf = imin(imax(b - base, 0), G);  // frozen columns in this window
+            const unsigned lowm = nf >= 32 ? 0xffffffffu : ((1u << nf) - 1u);
+            const unsigned fm = m & lowm;
+            if (fm) {
+                fmin = imin(fmin, base + __ffs(fm) - 1);
+                fmax = imax(fmax, base + 31 - __clz(fm));
+            }
+            if (m & ~lowm) tnz = true;
+            base += G;
+            if (base >= c) srch = false;
+        }
+    }
+}
+
 // Per-pair state, uniform across the pair's G lanes.
 struct PairState {
     DevPair *pp;
@@ -503,7 +535,7 @@ struct PairState {
 };
 
 template <int G, int K>
-__global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
+__global__ void __launch_bounds__(128, 5) bsw_kernel(LaunchArgs A) {
     TALBSW_DYNAMIC_SMEM(smem_raw);
     constexpr int NG = 32 / G;
     constexpr int SPAN = G * K;
@@ -720,19 +752,22 @@ __global__ void __launch_bounds__(128) bsw_kernel(LaunchArgs A) {
         // group-coupling detector: frozen columns, the row's scalar checks and
         // the old entries a group may trim
         if (det) {
-            const bool fz = rowact && ps.cp.frozenTo < beg;
-            const int f0 = scan_first_nz<G>(Hh, Fv, ps.cp.frozenTo, beg, fz, gl, gshift, gbits, wm);
-            const int f1 = scan_last_nz<G>(Hh, Fv, ps.cp.frozenTo, beg - 1, fz, gl, gshift, gbits, wm);
-            if (fz && f0 < beg) { ps.cp.frozen_nz(f0); ps.cp.frozen_nz(f1); }
-            if (rowact) ps.cp.frozenTo = imax(ps.cp.frozenTo, beg);
             const bool stay = rowact && !(i1 > ps.mlen || ps.tail == ps.head || ps.head > ps.tail);
-            if (rowact)
+            // one pass: columns freezing this row [frozenTo, beg), and the old
+            // entries a group may trim [beg, th) when the lane does not
+            const int th = stay ? imax(ps.cp.trim_hi(changed, end, ps.head), beg) : beg;
+            const int a = rowact ? imin(ps.cp.frozenTo, beg) : 0;
+            int fmin, fmax;
+            bool tnz;
+            scan_frozen_trim<G>(Hh, Fv, a, beg, th, rowact, gl, gshift, gbits, wm, fmin, fmax, tnz);
+            if (rowact) {
+                if (fmax >= 0) { ps.cp.frozen_nz(fmin); ps.cp.frozen_nz(fmax); }
+                ps.cp.frozenTo = imax(ps.cp.frozenTo, beg);
                 ps.cp.row_checks(true, i1 > ps.mlen, stay, i, ps.wk, beg, end, ps.ncol, h10init, hv_next,
                                  ps.is8 ? 127 : 32767);
-            const int th = stay ? ps.cp.trim_hi(changed, end, ps.head) : -1;
-            const int ft = scan_first_nz<G>(Hh, Fv, beg, th, stay && beg < th, gl, gshift, gbits, wm);
-            if (stay && beg < th && ft < th) ps.cp.flag |= CPL_TRIM;
-            if (rowact && ps.cp.flag) { drop(); rowact = false; }
+                if (stay && tnz) ps.cp.flag |= CPL_TRIM;
+                if (ps.cp.flag) { drop(); rowact = false; }
+            }
             __syncwarp();
         }
         // columns that left the band since the last row are frozen: note the

@@ -186,7 +186,14 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
     const int32_t *order = A.seg ? A.order + A.seg[0] : A.order;
     const int32_t *order_req = A.reqs ? (A.seg ? A.order_req + A.seg[0] : A.order_req) : nullptr;
     auto fail = [&](int flag, int req, int pidx) { report_error(A, req, flag, pidx); };
+    // a pair ends (exit, zero row, z-drop, last row): its outputs, or, when the
+    // detector flagged it during this row, its place on the flagged list
     auto finish = [&]() {
+        active = false;
+        if (det && s.cp.flag) {
+            flag_pair(A, s.req, s.pidx);
+            return;
+        }
         if (A.cells) atomicAdd(A.cells, s.ncells);
         s.pp->score = s.maxScore;
         s.pp->tle = s.x;
@@ -194,7 +201,6 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
         s.pp->max_off = s.max_off;
         s.pp->gscore = s.gscore;
         s.pp->gtle = s.max_ie;
-        active = false;
     };
 
     // One iteration = one row of this lane's pair; a lane that finishes a pair
@@ -352,7 +358,6 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                 for (int l = beg; l < hi; l++)
                     if (hf(l) != 0u) { s.cp.flag |= CPL_TRIM; break; }
             }
-            if (s.cp.flag) { flag_pair(A, s.req, s.pidx); active = false; continue; }
         }
         if (changed) {
             const int hi = imin(end, head);
@@ -389,7 +394,6 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
                 fe = Couple::fnext((int)(wv & 0xffffu), (int)(wv >> 16), lane_score1(tlo, thi, q), e_del, oe_del);
             }
             s.cp.f_checks(true, i, s.wk, beg, end, head, tail, ncol, s.is8 ? 127 : 32767, tin, ft, fe);
-            if (s.cp.flag) { flag_pair(A, s.req, s.pidx); active = false; continue; }
         }
 
         // ---- the band [beg, end): masked left part, clean middle, tail part
@@ -490,7 +494,6 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             if (det) {
                 if (!changed && oldnz_masked) s.cp.flag |= CPL_TRIM;  // the group may trim them
                 s.cp.stored_last(jl, ncol, (int)hst, tb >= 4 ? -1 : -P.b, head, tail, e_del, oe_del);
-                if (s.cp.flag) { flag_pair(A, s.req, s.pidx); active = false; continue; }
             }
         }
         // gscore at the query's last column (:3177-3195): in the band exactly

@@ -1,9 +1,10 @@
 // Exact scoring of the pairs the per-pair kernels flag (bsw_couple.cuh): the
 // reference scores a caller's array in SIMD groups of 32 (16-bit) / 64
 // (8-bit) consecutive pairs (bandedSWA.cpp:2722-2955 / :2030-2258); a flagged
-// pair's outputs may depend on the other pairs of its group, so its whole
-// group is scored again by the grouped kernel (bsw_group.cuh) and every
-// member's outputs are replaced by the grouped ones.
+// pair's outputs may depend on the other pairs of its group, so its group is
+// scored again by the block-wide grouped kernel (bsw_group_wide.cuh), which
+// stops once the group's flagged lanes have exited and writes their outputs
+// (the other members keep their per-pair outputs, equal to the grouped ones).
 //
 // A group is defined by the caller's array: the reference takes one band and
 // one precision per call, so a batch with per-pair bands and 8/16-bit routing
@@ -20,7 +21,7 @@
 #include <algorithm>
 
 #include "bsw_ctx.h"
-#include "bsw_group.cuh"
+#include "bsw_group_wide.cuh"
 
 namespace talbsw {
 
@@ -164,10 +165,12 @@ __global__ void __launch_bounds__(256) rg_mark(LaunchArgs A, int nreq, long long
         const long long rank = (long long)V.offsets[(size_t)c * V.nchunks + k] + intra;
         const int bits = V.cinfo[c].z;
         const long long grp = rank / group_lanes(bits);
+        const unsigned long long lbit = 1ull << (int)(rank % group_lanes(bits));
         const unsigned long long gkey = ((unsigned long long)c << 40) | (unsigned long long)grp;
         unsigned s = (unsigned)mix64(gkey) & (unsigned)(V.hcap - 1);
         for (int probe = 0; probe < V.hcap; probe++) {
             const unsigned long long old = atomicCAS(&V.mhash[s], kEmpty, gkey);
+            if (old == kEmpty || old == gkey) atomicOr(&V.needh[s], lbit);  // this pair's lane is wanted
             if (old == kEmpty) {
                 const int b = bits == 8 ? 1 : 0;
                 const int m = atomicAdd(&V.ctr[1 + b], 1);
@@ -239,7 +242,10 @@ __global__ void __launch_bounds__(256) rg_gather(LaunchArgs A, int nreq, long lo
             if (k < nck) run = max(run, (long long)off[k]);
         }
         padq = __reduce_max_sync(0xffffffffu, padq);
-        if (lane == 0) V.ginfo[slot] = make_int4(ci.x, ci.y, padq, 0);
+        if (lane == 0) {
+            V.ginfo[slot] = make_int4(ci.x, ci.y, padq, 0);
+            V.gneed[slot] = V.needh[V.mslot[slot]];
+        }
     }
 }
 
@@ -251,6 +257,7 @@ __global__ void rg_cleanup(RegroupView V) {
     for (int e = tid; e < n16 + n8; e += nth) {
         const size_t slot = e < n16 ? (size_t)e : (size_t)V.mcap + (e - n16);
         V.mhash[V.mslot[slot]] = kEmpty;
+        V.needh[V.mslot[slot]] = 0ull;
     }
     for (int c = tid; c < kRegroupClasses; c += nth) V.ckeys[c] = kEmpty;
 }
@@ -280,11 +287,19 @@ cudaError_t RegroupBufs::ensure(long long ntotal, int cols_cap, int num_sms, boo
     // group-kernel scratch: slots for the longer of the 16- and 8-bit rows
     const int col_cap = std::max(cols_cap, 1) + 3;
     const long long slot_bytes = (long long)std::max(group_slot_elems(col_cap, 16), group_slot_elems(col_cap, 8)) * 2;
-    long long warps = std::min<long long>((long long)num_sms * 8, std::max<long long>(4, (1LL << 30) / slot_bytes));
-    warps = (warps + 3) & ~3LL;
+    // one global slot per block, for the groups whose rows do not fit shared memory
+    const long long slots = std::min<long long>((long long)num_sms, std::max<long long>(4, (1LL << 30) / slot_bytes));
     if (nchunks <= V.nchunks && fcap <= V.fcap && col_cap <= V.col_cap && V.ctr) {
         return cudaSuccess;
     }
+    // the block-wide kernel: one block per group, the group's rows in shared
+    // memory up to the opt-in limit (one block per SM)
+    int dev = 0, optin = 0;
+    cudaError_t e0 = cudaGetDevice(&dev);
+    if (e0 == cudaSuccess) e0 = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e0 == cudaSuccess) e0 = cudaFuncSetAttribute(bsw_group_wide_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e0 == cudaSuccess) e0 = cudaFuncSetAttribute(bsw_group_wide_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e0 != cudaSuccess) return e0;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
     const size_t o_ctr = take(sizeof(int) * 8);
@@ -297,11 +312,13 @@ cudaError_t RegroupBufs::ensure(long long ntotal, int cols_cap, int num_sms, boo
     const size_t o_off = take(sizeof(int) * kRegroupClasses * nchunks);
     const size_t o_tot = take(sizeof(int) * kRegroupClasses);
     const size_t o_mh = take(sizeof(unsigned long long) * hcap);
+    const size_t o_nh = take(sizeof(unsigned long long) * hcap);
+    const size_t o_gn = take(sizeof(unsigned long long) * 2 * mcap);
     const size_t o_ml = take(sizeof(int2) * 2 * mcap);
     const size_t o_ms = take(sizeof(int) * 2 * mcap);
     const size_t o_mem = take(sizeof(long long) * 64 * 2 * mcap);
     const size_t o_gi = take(sizeof(int4) * 2 * mcap);
-    const size_t o_scr = take((size_t)warps * (size_t)slot_bytes);
+    const size_t o_scr = take((size_t)slots * (size_t)slot_bytes);
     arena.release();
     cudaError_t e = arena.ensure(off);
     if (e != cudaSuccess) { V = RegroupView(); return e; }
@@ -316,6 +333,8 @@ cudaError_t RegroupBufs::ensure(long long ntotal, int cols_cap, int num_sms, boo
     V.offsets = reinterpret_cast<int *>(b + o_off);
     V.totals = reinterpret_cast<int *>(b + o_tot);
     V.mhash = reinterpret_cast<unsigned long long *>(b + o_mh);
+    V.needh = reinterpret_cast<unsigned long long *>(b + o_nh);
+    V.gneed = reinterpret_cast<unsigned long long *>(b + o_gn);
     V.mlist = reinterpret_cast<int2 *>(b + o_ml);
     V.mslot = reinterpret_cast<int *>(b + o_ms);
     V.members = reinterpret_cast<long long *>(b + o_mem);
@@ -326,11 +345,13 @@ cudaError_t RegroupBufs::ensure(long long ntotal, int cols_cap, int num_sms, boo
     V.mcap = (int)mcap;
     V.hcap = (int)hcap;
     V.col_cap = col_cap;
-    V.warps = (int)warps;
+    V.slots = (int)slots;
+    V.smem = optin;
     // empty tables, zero counters (the passes leave them so)
     if ((e = cudaMemset(V.ctr, 0, sizeof(int) * 8)) != cudaSuccess) return e;
     if ((e = cudaMemset(V.ckeys, 0xff, sizeof(unsigned long long) * kRegroupClasses)) != cudaSuccess) return e;
     if ((e = cudaMemset(V.mhash, 0xff, sizeof(unsigned long long) * hcap)) != cudaSuccess) return e;
+    if ((e = cudaMemset(V.needh, 0, sizeof(unsigned long long) * hcap)) != cudaSuccess) return e;
     *grown = true;
     return cudaDeviceSynchronize();
 }
@@ -364,13 +385,16 @@ cudaError_t enqueue_regroup(const RegroupView &V, LaunchArgs A, int nreq, long l
         G.P = A.P;
         G.members = V.members + (size_t)b * V.mcap * 64;
         G.ginfo = V.ginfo + (size_t)b * V.mcap;
+        G.need = V.gneed + (size_t)b * V.mcap;
         G.ngroups_dev = &V.ctr[1 + b];
         G.ngroups_cap = V.mcap;
         G.reqs = A.reqs;
         G.nreq = nreq;
-        const int blocks = V.warps / 4;
-        if (b == 0) bsw_group_kernel<16><<<blocks, 128, 0, s>>>(G);
-        else bsw_group_kernel<8><<<blocks, 128, 0, s>>>(G);
+        G.smem_bytes = (size_t)V.smem;
+        // one block per group at a time; a block's global slot is its index
+        const int blocks = std::min(V.slots, num_sms);
+        if (b == 0) bsw_group_wide_kernel<16><<<blocks, 32 * kWideWarps, V.smem, s>>>(G);
+        else bsw_group_wide_kernel<8><<<blocks, 32 * kWideWarps, V.smem, s>>>(G);
     }
     rg_cleanup<<<std::max(1, num_sms), 256, 0, s>>>(V);
     rg_reset<<<1, 32, 0, s>>>(V, A.err_flags, A.reqs, nreq);

@@ -25,7 +25,8 @@ TAL_OK, TAL_EINVAL, TAL_EDOMAIN, TAL_ENOMEM, TAL_ECUDA, TAL_ETIMEOUT, TAL_ENODEV
 STATUS_NAMES = {0: "TAL_OK", 1: "TAL_EINVAL", 2: "TAL_EDOMAIN", 3: "TAL_ENOMEM", 4: "TAL_ECUDA",
                 5: "TAL_ETIMEOUT", 6: "TAL_ENODEV", 7: "TAL_EBUSY"}
 AUTO, BITS8, BITS16 = 0, 8, 16
-GROUPED = 0x100  # OR into BITS8 / BITS16: the reference's SIMD groups, exactly
+GROUPED = 0x100  # OR into BITS8 / BITS16: every pair in the reference's SIMD groups (same outputs, slower)
+PER_PAIR = 0x200  # OR in: every pair alone in its group (scalarBandedSWAWrapper's semantics)
 
 
 class TalBswError(RuntimeError):
@@ -161,14 +162,16 @@ class BandedPairWiseSW:
     # -- reference entry points -------------------------------------------------
     def getScores8(self, pairArray, seqBufRef, seqBufQer, numPairs: int, numThreads: int = 1,
                    w: int = 100, grouped: bool = False) -> None:
-        """grouped: score in the reference's groups of 64 consecutive pairs
-        (equal to the reference's outputs on any input; slower)."""
+        """Outputs equal the reference's on any input (pairs whose outputs
+        depend on their SIMD group are re-scored in it).  grouped: compute
+        every pair in the reference's groups of 64 (same outputs, slower)."""
         self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, BITS8 | (GROUPED if grouped else 0))
 
     def getScores16(self, pairArray, seqBufRef, seqBufQer, numPairs: int, numThreads: int = 1,
                     w: int = 100, grouped: bool = False) -> None:
-        """grouped: score in the reference's groups of 32 consecutive pairs
-        (equal to the reference's outputs on any input; slower)."""
+        """Outputs equal the reference's on any input (pairs whose outputs
+        depend on their SIMD group are re-scored in it).  grouped: compute
+        every pair in the reference's groups of 32 (same outputs, slower)."""
         self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, BITS16 | (GROUPED if grouped else 0))
 
     def getScoresAuto(self, pairArray, seqBufRef, seqBufQer, numPairs: int,
@@ -176,6 +179,27 @@ class BandedPairWiseSW:
         """Each pair to the 8-bit kernel when it is inside the 8-bit range,
         else to the 16-bit kernel."""
         self._scores(pairArray, seqBufRef, seqBufQer, numPairs, w, AUTO)
+
+    def scalarBandedSWAWrapper(self, seqPairArray, seqBufRef, seqBufQer, numPairs: int,
+                               nthreads: int = 1, w: int = 100) -> None:
+        """bandedSWA.cpp:242-260: every pair scored on its own.  Runs on the GPU
+        where the scalar path equals the vector kernels for a pair alone
+        (e_del = e_ins = 1; the scoring matrix of bench-bsw, which this class
+        assumes), else raises."""
+        if self.params["e_del"] != 1 or self.params["e_ins"] != 1:
+            raise TalBswError(TAL_EINVAL, "the scalar path runs on the GPU only with e_del = e_ins = 1")
+        self._scores(seqPairArray, seqBufRef, seqBufQer, numPairs, w, BITS16 | PER_PAIR)
+
+    def scalarBandedSWA(self, qlen: int, query, tlen: int, target, w: int, h0: int):
+        """bandedSWA.cpp:116-237 for one pair: returns (score, qle, tle, gtle,
+        gscore, max_off)."""
+        from .seqpair import new_pairs
+        p = new_pairs(1)
+        p["len1"], p["len2"], p["h0"] = tlen, qlen, h0
+        self.scalarBandedSWAWrapper(p, np.ascontiguousarray(target, np.uint8),
+                                    np.ascontiguousarray(query, np.uint8), 1, 1, w)
+        r = p[0]
+        return int(r["score"]), int(r["qle"]), int(r["tle"]), int(r["gtle"]), int(r["gscore"]), int(r["max_off"])
 
     # -- device-resident form -------------------------------------------------------
     def scores_device(self, d_pairs: int, d_ref: int, ref_bytes: int, d_qer: int, qer_bytes: int,
