@@ -237,13 +237,21 @@ int tal_bsw_probe_int_peak(int device, double *dpx_per_s, double *i32_per_s);
  * this entry point does not; on those pairs its outputs are the pair's own.
  * Status: TAL_EDOMAIN for a pair outside the per-pair kernels' exact range
  * (including wrapping values) or with a base code above 4, TAL_ENOMEM for a
- * pair whose rows do not fit the kernels' shared memory; the offending pair
- * is not named here (the handle entry points report it through
- * tal_bsw_last_bad_pair). */
+ * pair whose rows do not fit the kernels' shared memory (checked on the
+ * device per pair, or for the whole batch before the launch);
+ * tal_bsw_noalloc_last_bad_pair names the offending pair. */
 int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_seq_pair *d_pairs,
                                   const uint8_t *d_ref, size_t ref_bytes,
                                   const uint8_t *d_qer, size_t qer_bytes, int32_t numPairs,
                                   int32_t w, const int32_t *d_w, int bits, void *stream);
+
+/* The lowest index of a pair that made the last tal_bsw_scores_device_noalloc
+ * call on the current device fail (TAL_EDOMAIN, or TAL_ENOMEM found on the
+ * device); -1 after a successful call or when the failure names no pair (the
+ * batch's longest rows exceed shared memory before any launch), and before
+ * the first call.  Reads host memory only; same serialisation rule as the
+ * scoring call. */
+int64_t tal_bsw_noalloc_last_bad_pair(void);
 
 /* ---------------------------------------------------------------------------
  * Serving loop; no counterpart in the reference, whose callers block in one

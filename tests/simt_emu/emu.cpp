@@ -260,7 +260,7 @@ extern "C" int emu_bsw_group_wide_run(talbsw::DevPair *pairs, const uint8_t *ref
     int m2 = 1;
     for (int i = 0; i < n; i++) m2 = std::max(m2, pairs[i].len2);
     G.col_cap = m2 + 3;
-    G.slot_elems = talbsw::group_slot_elems(G.col_cap, bits);
+    G.slot_elems = talbsw::wide_slot_elems(G.col_cap, bits);
     std::vector<int16_t> scratch(G.slot_elems, (int16_t)0x5a5a);  // poisoned
     G.scratch = scratch.data();
     int counter = 0, ng = ngroups;

@@ -65,6 +65,13 @@ def test_noalloc_matches_regular_entry_point(name, bits):
     assert (outputs(exp) == outputs(got[k])).all(), "noalloc slice differs from the oracle"
 
 
+def _last_bad(lib):
+    f = lib.tal_bsw_noalloc_last_bad_pair
+    f.restype = ctypes.c_int64
+    f.argtypes = []
+    return int(f())
+
+
 def test_noalloc_reports_out_of_range_pairs():
     import torch
     b = synth.generate(synth.C1, 64)     # 151 bp: outside the 8-bit range
@@ -74,12 +81,40 @@ def test_noalloc_reports_out_of_range_pairs():
     d_ref = torch.from_numpy(b.ref).cuda()
     d_qer = torch.from_numpy(b.qer).cuda()
     assert _noalloc(lib, P, d_pairs, d_ref, d_qer, b.n, 100, 8) == tal_bsw.api.TAL_EDOMAIN
-    # a base code above 4 is a domain error too
+    assert _last_bad(lib) == 0  # every pair is out of range: the lowest index
+    # a base code above 4 is a domain error too, naming its pair
     q = b.qer.copy()
     q[int(b.pairs["idq"][5]) + 1] = 9
     d_q9 = torch.from_numpy(q).cuda()
     d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
     assert _noalloc(lib, P, d_pairs, d_ref, d_q9, b.n, 100, 16) == tal_bsw.api.TAL_EDOMAIN
+    assert _last_bad(lib) == 5
     # the next call clears the shared control block and succeeds
     d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
     assert _noalloc(lib, P, d_pairs, d_ref, d_qer, b.n, 100, 16) == tal_bsw.api.TAL_OK
+    assert _last_bad(lib) == -1
+
+
+def test_noalloc_capacity_is_not_a_domain_error():
+    """A pair inside the exact range whose rows exceed shared memory (a
+    30,000-base query with a band covering it, whole rows of the G-lane
+    kernel): TAL_ENOMEM, not TAL_EDOMAIN, and no pair named (the batch is
+    refused before the launch)."""
+    import torch
+    rng = np.random.default_rng(3)
+    L = 30000
+    q = rng.integers(0, 4, L).astype(np.uint8)
+    r = q.copy()
+    pairs = np.zeros(1, tal_bsw.SEQPAIR_DTYPE)
+    pairs["idr"] = 0
+    pairs["idq"] = 0
+    pairs["len1"] = L
+    pairs["len2"] = L
+    pairs["h0"] = 10
+    P = synth.C2.params()
+    lib = tal_bsw.api.core_lib()
+    d_pairs = torch.from_numpy(pairs.view(np.uint8).copy()).cuda()
+    d_ref = torch.from_numpy(r).cuda()
+    d_qer = torch.from_numpy(q).cuda()
+    assert _noalloc(lib, P, d_pairs, d_ref, d_qer, 1, L, 16) == tal_bsw.api.TAL_ENOMEM
+    assert _last_bad(lib) == -1

@@ -415,9 +415,13 @@ int autotune(tal_bsw_ctx *h, const LaunchArgs &base, int n, int w) {
         for (const KConfig &k : cands) {
             if (config_smem(k, cols, 1, win) > h->smem_optin) continue;
             LaunchArgs A = seg_launch_args(h, tsb, base, sg, ts[1]);
+            // timed with the coupling detector on, as the captured launches run
+            // (its flags are dropped: the sample's outputs are scored again)
+            attach_regroup(A, h->regroup.V);
             float ms = 1e30f;
             for (int rep = 0; rep < 2 && e == cudaSuccess; rep++) {
                 e = cudaMemsetAsync(&c->counter[sg], 0, sizeof(int), h->stream);
+                if (e == cudaSuccess) e = cudaMemsetAsync(h->regroup.V.ctr, 0, sizeof(int), h->stream);
                 if (e != cudaSuccess) break;
                 cudaEventRecord(e0, h->stream);
                 e = launch_config(A, k, h->num_sms, h->smem_optin, h->stream);
@@ -438,6 +442,7 @@ int autotune(tal_bsw_ctx *h, const LaunchArgs &base, int n, int w) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->regroup.V.ctr, 0, sizeof(int), h->stream);
     if (e != cudaSuccess) return bfail(h, TAL_ECUDA, std::string("autotune: ") + cudaGetErrorString(e));
     h->tuned = true;
     return TAL_OK;
@@ -533,7 +538,7 @@ int batched_device_locked(tal_bsw_ctx *h, tal_seq_pair *d_pairs, const uint8_t *
         ge.exec = exec;
         it = h->graphs.emplace(key, ge).first;
     } else {
-        h->launches += 4 + kNumSegs + 10;
+        h->launches += 4 + kNumSegs + 11;
     }
     e = cudaGraphLaunch(it->second.exec, h->stream);
     if (e != cudaSuccess) return bfail(h, TAL_ECUDA, std::string("graph launch: ") + cudaGetErrorString(e));

@@ -123,7 +123,12 @@ struct BatchCtrl {
 // counters, [5] overflow bits; [6] / [7] the last pass's flagged pairs and
 // re-scored groups.
 constexpr int kRegroupClasses = 1024;  // distinct classes among one call's flagged pairs
-constexpr int kRegroupChunk = 2048;    // pairs per counting chunk
+constexpr int kRegroupChunk = 2048;
+// Shared memory of the regroup pass's first scoring launch: up to three blocks
+// per SM, room (after the 12.5 KB of cross-warp exchange) for a 16-bit group's
+// 256-column ring (bands up to 124) with its frozen-column record up to ~5,300
+// columns, or an 8-bit group's whole rows.
+constexpr int kRegroupSmem1 = 75 * 1024;    // pairs per counting chunk
 struct RegroupView {
     int *ctr = nullptr;
     long long *flagged = nullptr;
@@ -140,7 +145,9 @@ struct RegroupView {
     long long *members = nullptr;
     int4 *ginfo = nullptr;
     int16_t *scratch = nullptr;
-    int nchunks = 0, fcap = 0, mcap = 0, hcap = 0, col_cap = 0, slots = 0, smem = 0;
+    int nchunks = 0, fcap = 0, mcap = 0, hcap = 0, col_cap = 0, slots = 0;
+    int smem = 0;          // the second scoring launch's shared memory (the opt-in limit)
+    int smem1 = 0, grid1[2] = {0, 0};  // the first launch's (16-, 8-bit): several blocks per SM
 };
 struct RegroupBufs {
     DevBuf arena;

@@ -57,6 +57,11 @@ struct GroupArgs {
     const unsigned long long *need = nullptr;  // per group, the lanes whose outputs are
                                                // wanted (bit l: lane l; null: all)
     size_t smem_bytes = 0;  // the block-wide kernel's dynamic shared memory per block
+    // block-wide kernel in two launches: the first (defer) leaves the groups
+    // whose rows do not fit its shared memory, the second skips the groups
+    // whose rows need at most skip_upto bytes (the first launch took them)
+    bool defer = false;
+    size_t skip_upto = 0;
 };
 
 // Global pair index -> (request, local index) in a serving tick's pair space.

@@ -44,7 +44,7 @@
 
 namespace talbsw {
 
-constexpr int kWideWarps = 4;  // warps per group
+constexpr int kWideWarps = 8;  // warps per group (4 measured 6.2 against 3.2 ms for C2's regroup pass)
 
 // Cross-warp exchange of one block, at the start of its shared memory.
 template <int NW>
@@ -67,9 +67,11 @@ __host__ __device__ constexpr size_t wide_x_bytes() {
     return (sizeof(WideX<NW>) + 15) & ~(size_t)15;
 }
 
-// Shared memory of a block whose group rows hold col_cap columns.
-__host__ __device__ inline size_t wide_smem_bytes(int col_cap, int bits) {
-    return wide_x_bytes<kWideWarps>() + group_smem_bytes(col_cap, bits);
+// int16 elements of a block's global slot: whole rows of col_cap columns as
+// in group_slot_elems, then the per-column masks of non-zero lanes.
+__host__ __device__ inline size_t wide_slot_elems(int col_cap, int bits) {
+    const size_t lpt = bits == 8 ? 2 : 1;
+    return group_slot_elems(col_cap, bits) + ((size_t)col_cap * 4 * lpt + 32) / 2 + 8;
 }
 
 template <int SB, int NW>
@@ -190,50 +192,33 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
         const int minq = __reduce_min_sync(full, mq) - 1;
         const int nrow = maxLen1, ncol = maxLen2, wrapRows = maxLen1;
         const int colCap = (ncol > 1 ? ncol : 1) + 3;
-        uint32_t *const HF = group_smem_bytes(colCap, SB) <= rows_bytes ? smRows : HFg;
-        int8_t *const Q2 = reinterpret_cast<int8_t *>(HF + (size_t)colCap * W);
-        auto HFa = [&](int c, int u) -> uint32_t & { return HF[(size_t)c * W + t + 32 * u]; };
-        auto code_at = [&](int c, int u) -> int {
-            return Q2[(((size_t)(c >> 2) * W + t + 32 * u) << 2) + (c & 3)];
-        };
-        auto pack = [](int h, int f) -> uint32_t { return (uint32_t)(uint16_t)h | ((uint32_t)(uint16_t)f << 16); };
 
-        // ---- per-lane set-up: query codes and the first row, columns split
-        // over the warps (the first row's gap values in closed form), band clamp
-        int h0[LPT], tlen[LPT], qlen[LPT], myband[LPT];
+        // ---- per-lane set-up: band clamp, query bases checked
+        int h0[LPT], tlen[LPT], qlen[LPT], myband[LPT], tt1[LPT], tt2[LPT];
+        const uint8_t *qp[LPT];
         int bsz = gw;
         for (int u = 0; u < LPT; u++) {
             const int l = t + 32 * u;
             h0[u] = E::ws((int)E::us(h0r[u]));
             tlen[u] = E::ws((int)E::us(len1[u]));
             qlen[u] = E::ws((int)E::us(len2[u]));
-            const uint8_t *q = real[u] ? Aqer + (idq[u] - qer_lo)
-                             : (qer_lo <= 0 && len2[u] <= qer_hi) ? Aqer - qer_lo : nullptr;
+            // a padding lane (8-bit) reads the query bytes at the caller's
+            // offset 0, as the reference's zeroed SeqPair does
+            qp[u] = real[u] ? Aqer + (idq[u] - qer_lo)
+                  : (qer_lo <= 0 && len2[u] <= qer_hi) ? Aqer - qer_lo : nullptr;
             // row 0: h0, tt1 = h0 - oe_ins (wrapped), then the reference's chain
             // tt = max(tt - e_ins, 0) below the group's longest query; from
             // column 2 on the chain starts from a value >= 0 and no longer
             // wraps, so column k holds max(tt2 - (k - 2) e_ins, 0)
-            const int tt1 = (h0[u] > oe_ins) ? E::ws(h0[u] - oe_ins) : 0;
-            const int tt2 = imax(E::ws(tt1 - e_ins), 0);
-            for (int k = wp; k < colCap; k += NW) {
-                int code = 0;
-                if (k < len2[u]) {
-                    const int b = q ? q[k] : 4;
-                    if (b > 4 && real[u]) {
+            tt1[u] = (h0[u] > oe_ins) ? E::ws(h0[u] - oe_ins) : 0;
+            tt2[u] = imax(E::ws(tt1[u] - e_ins), 0);
+            if (real[u] && qp[u])
+                for (int k = wp; k < len2[u]; k += NW)
+                    if (qp[u][k] > 4) {
                         gerr(ERR_BASE, lidx[u]);
                         bad = true;
+                        break;
                     }
-                    code = b == 4 ? -1 : E::ws(b);
-                } else if (k <= maxLen2) {
-                    code = 100;  // DUMMY2 (:46)
-                }
-                Q2[(((size_t)(k >> 2) * W + l) << 2) + (k & 3)] = (int8_t)code;
-                int hv = 0;
-                if (k == 0) hv = h0[u];
-                else if (k == 1) hv = tt1;
-                else if (k < maxLen2) hv = imax(tt2 - (k - 2) * e_ins, 0);
-                HF[(size_t)k * W + l] = (uint16_t)hv;
-            }
             // band clamp (:2882-2904 / :2183-2205): integer division, then +1.0
             const int qlenb = E::ws(len2[u] * maxsc);
             const int eb_ins = E::ws(P.end_bonus - P.o_ins), eb_del = E::ws(P.end_bonus - P.o_del);
@@ -256,6 +241,65 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
         __syncthreads();
         if (X.bad) continue;
         const int w = __reduce_max_sync(full, bsz);
+
+        // ---- the group's rows.  Row i touches columns up to i + w + 3 (its
+        // band end, the last-column store, the scans' end) and writes none
+        // below its band start beg >= i - w, which never decreases.  So the
+        // rows live in a ring of WR >= 2w + 8 columns (column c in slot
+        // c mod WR) when that is shorter than the query, whole rows when not,
+        // and in the block's global slot when neither fits shared memory.
+        // Beside them, for every column, the mask of lanes whose (H, F) word
+        // is non-zero (NZ), kept current at every store: the narrowing and
+        // the head / tail scans read only those masks, so a column that left
+        // the band needs no slot once its last store is recorded.
+        int WR = 8;
+        while (WR < 2 * w + 8) WR <<= 1;
+        bool ring = WR < colCap;
+        if (!ring) WR = colCap;
+        const size_t nz_bytes = (size_t)colCap * 4 * LPT + 32;
+        const size_t rows_need = (ring ? (size_t)WR * W * 5 : group_smem_bytes(colCap, SB)) + nz_bytes;
+        if (rows_need <= A.skip_upto) continue;             // the first launch scored it
+        if (A.defer && rows_need > rows_bytes) continue;  // the second launch will
+        uint32_t *HF = smRows;
+        if (rows_need > rows_bytes) {
+            ring = false;
+            WR = colCap;
+            HF = HFg;
+        }
+        const int wm = WR - 1;
+        int8_t *const Q2 = reinterpret_cast<int8_t *>(HF + (size_t)WR * W);
+        uint32_t *const NZ = reinterpret_cast<uint32_t *>(
+            reinterpret_cast<uintptr_t>(Q2 + ((((size_t)WR + 3) & ~(size_t)3) + 8) * W + 15) & ~(uintptr_t)15);
+        auto slot = [&](int c) -> int { return ring ? (c & wm) : c; };
+        auto HFa = [&](int c, int u) -> uint32_t & { return HF[(size_t)slot(c) * W + t + 32 * u]; };
+        auto code_at = [&](int c, int u) -> int {
+            const int sc = slot(c);
+            return Q2[(((size_t)(sc >> 2) * W + t + 32 * u) << 2) + (sc & 3)];
+        };
+        auto pack = [](int h, int f) -> uint32_t { return (uint32_t)(uint16_t)h | ((uint32_t)(uint16_t)f << 16); };
+        // column k's query code and row-0 entry, for every lane of this thread
+        auto init_col = [&](int k) {
+            const int sc = slot(k);
+            for (int u = 0; u < LPT; u++) {
+                const int l = t + 32 * u;
+                int code = 0;
+                if (k < len2[u]) {
+                    const int b = qp[u] ? qp[u][k] : 4;
+                    code = b == 4 ? -1 : E::ws(b);
+                } else if (k <= maxLen2) {
+                    code = 100;  // DUMMY2 (:46)
+                }
+                Q2[(((size_t)(sc >> 2) * W + l) << 2) + (sc & 3)] = (int8_t)code;
+                int hv = 0;
+                if (k == 0) hv = h0[u];
+                else if (k == 1) hv = tt1[u];
+                else if (k < maxLen2) hv = imax(tt2[u] - (k - 2) * e_ins, 0);
+                HF[(size_t)sc * W + l] = (uint16_t)hv;
+                const unsigned m = __ballot_sync(full, (uint16_t)hv != 0);
+                if (t == 0) NZ[(size_t)k * LPT + u] = m;
+            }
+        };
+        int initc = 0;  // next column to initialise
 
         // ---- the kernel proper (:2962-3356 / :2263-2661)
         int head[LPT], tail[LPT], mlen[LPT], maxScore[LPT], x[LPT], y[LPT];
@@ -310,9 +354,21 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                 tail[u] = E::ws((int)tu);
                 changed |= head[u] != ph || tail[u] != pt;
             }
+            // columns coming within reach: query codes and row-0 entries.  From
+            // row 1 on they lie past the band end, and the ring slots they take
+            // belong to columns below the previous row's band start, which no
+            // row reads or writes again; so none of this races with the trimming
+            const int lim = imin(colCap - 1, i + w + 3);
+            const bool ini = initc <= lim;
+            if (ini) {
+                for (int k = initc + wp; k <= lim; k += NW) init_col(k);
+                initc = lim + 1;
+            }
             // trimming (:3091-3112): the sequential pass stops at the first
             // column no lane's head is beyond, so it covers [beg, max head)
-            if (__any_sync(full, changed)) {
+            const bool trim = __any_sync(full, changed);
+            if (trim) {
+                if (i == 0) __syncthreads();  // row 0 may trim columns it has just initialised
                 int mh = INT_MIN;
                 for (int u = 0; u < LPT; u++) mh = imax(mh, head[u]);
                 mh = __reduce_max_sync(full, mh);
@@ -322,8 +378,8 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                     for (int u = 0; u < LPT; u++)
                         if (head[u] > pj || jn > tail[u]) HFa(lc, u) = 0;
                 }
-                __syncthreads();
             }
+            if (ini || trim) __syncthreads();
             // row exit status (:3119-3129)
             bool need_live = false;
             for (int u = 0; u < LPT; u++) {
@@ -337,21 +393,28 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
             const int n = end > beg ? end - beg : 0;
             const int cs = (n + NW - 1) / NW;
             const int c0 = beg + imin(n, wp * cs), c1 = beg + imin(n, (wp + 1) * cs);
-            auto m11_of = [&](int j, int u, int h00) -> int {
-                const int a2 = code_at(j, u);
+            auto m11_of = [&](int a2, int u, int h00) -> int {
                 int sbt = s1[u] == a2 ? w_match : w_mismatch;
                 if ((s1[u] | a2) < 0) sbt = -1;  // an N on either side
                 const int m11 = E::ws(h00 + sbt);
                 return h00 == 0 ? 0 : m11;
             };
-            // pass 1: E over the chunk from 0
+            // pass 1: E over the chunk from 0 (the next column's word and code
+            // loaded one column ahead)
             if (c1 > c0) {
                 for (int u = 0; u < LPT; u++) {
                     int el = 0;
+                    uint32_t hfn = HFa(c0, u);
+                    int an = code_at(c0, u);
                     for (int j = c0; j < c1; j++) {
-                        const uint32_t hf = HFa(j, u);
+                        const uint32_t hf = hfn;
+                        const int a2 = an;
+                        if (j + 1 < c1) {
+                            hfn = HFa(j + 1, u);
+                            an = code_at(j + 1, u);
+                        }
                         const int h00 = (int16_t)(hf & 0xffffu), f11 = (int16_t)(hf >> 16);
-                        const int m11 = m11_of(j, u, h00);
+                        const int m11 = m11_of(a2, u, h00);
                         if (j == c1 - 1) {
                             X.Elast[wp][t + 32 * u] = el;
                             X.MF[wp][t + 32 * u] = imax(m11, f11);
@@ -382,15 +445,26 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                         h10[u] = imax(X.MF[wp - 1][l], el);
                     }
                 }
+                uint32_t hfn[LPT];
+                int an[LPT];
+                for (int u = 0; u < LPT; u++) {
+                    hfn[u] = HFa(c0, u);
+                    an[u] = code_at(c0, u);
+                }
                 for (int j = c0; j < c1; j++) {
                     const int pj = E::ws(j);
                     const int jn = E::ws(j + 1);
-                    bool nz = false;
+                    unsigned nzc = 0;
                     for (int u = 0; u < LPT; u++) {
                         const int l = t + 32 * u;
-                        const uint32_t hf = HFa(j, u);
+                        const uint32_t hf = hfn[u];
+                        const int a2 = an[u];
+                        if (j + 1 < c1) {  // next column's inputs (never this column's store)
+                            hfn[u] = HFa(j + 1, u);
+                            an[u] = code_at(j + 1, u);
+                        }
                         const int h00 = (int16_t)(hf & 0xffffu), f11 = (int16_t)(hf >> 16);
-                        const int m11 = m11_of(j, u, h00);
+                        const int m11 = m11_of(a2, u, h00);
                         int h11 = m11 > e11[u] ? m11 : e11[u];
                         h11 = h11 > f11 ? h11 : f11;
                         int tv = E::ws(m11 - oe_ins);
@@ -414,7 +488,9 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                         }
                         const uint32_t word = pack(hst, f21);
                         HFa(j, u) = word;
-                        nz |= word != 0u;
+                        const unsigned m = __ballot_sync(full, word != 0u);
+                        if (t == 0) NZ[(size_t)j * LPT + u] = m;
+                        nzc |= m;
                         h10[u] = h11;
                         // end-to-end score (:3178-3195), in the query's last column
                         if (j >= minq && jn == qlen[u] && exit0[u] < 0 && !(jn > tail[u]) &&
@@ -423,7 +499,7 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                             X.max_ie[l] = i1;
                         }
                     }
-                    if (__any_sync(full, nz)) {
+                    if (nzc) {
                         if (fnz == INT_MAX) fnz = j;
                         lnz = j;
                     }
@@ -440,17 +516,19 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
             if (wp == lw) {
                 const int j = beg > end ? beg : end;
                 const int j512 = E::ws(j);
+                unsigned nzc = 0;
                 if (j < colCap) {
                     for (int u = 0; u < LPT; u++) {
                         const bool m = head[u] > j512 || j512 > tail[u];
-                        HFa(j, u) = pack(m ? 0 : h10[u], 0);
+                        const uint32_t word = pack(m ? 0 : h10[u], 0);
+                        HFa(j, u) = word;
+                        const unsigned b = __ballot_sync(full, word != 0u);
+                        if (t == 0) NZ[(size_t)j * LPT + u] = b;
+                        nzc |= b;
                     }
                 }
-                bool nz = false;
-                if (end >= beg)
-                    for (int u = 0; u < LPT; u++) nz |= HFa(end, u) != 0u;
-                const bool any = __any_sync(full, nz);
-                if (t == 0) X.endnz = any;
+                // column end (== j when end >= beg) after the row, for the narrowing
+                if (t == 0) X.endnz = end >= beg && nzc != 0;
             }
             ncells += (unsigned long long)n;
             __syncthreads();
@@ -507,21 +585,26 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
             }
             if (is16) { beg = nbeg; end = nend; }
             // per-lane head / tail (:3265-3316 / :2571-2621): each warp scans a
-            // part and stops where no live lane is zero
+            // part of the range on the columns' masks and stops where no live
+            // lane is zero
             {
                 const int B = beg, Ee = end;
-                auto zero_at = [&](int c, int u) { return exit0[u] != 0 && HFa(c, u) == 0u; };
+                unsigned liveM[LPT];  // lanes still live (a zero there counts)
+                for (int u = 0; u < LPT; u++) liveM[u] = __ballot_sync(full, exit0[u] != 0);
                 const int mh = Ee > B ? Ee - B : 0;
                 const int ch = (mh + NW - 1) / NW;
                 const int p0 = B + imin(mh, wp * ch), p1 = B + imin(mh, (wp + 1) * ch);
                 int Zk = INT_MAX, Rk[LPT];
                 for (int u = 0; u < LPT; u++) Rk[u] = INT_MAX;
                 for (int lc = p0; lc < p1; lc++) {
-                    bool zl[LPT], any = false;
-                    for (int u = 0; u < LPT; u++) { zl[u] = zero_at(lc, u); any |= zl[u]; }
-                    if (!__any_sync(full, any)) { Zk = lc; break; }
+                    unsigned zl[LPT], any = 0;  // live lanes holding a zero word at lc
+                    for (int u = 0; u < LPT; u++) {
+                        zl[u] = liveM[u] & ~NZ[(size_t)lc * LPT + u];
+                        any |= zl[u];
+                    }
+                    if (!any) { Zk = lc; break; }
                     for (int u = 0; u < LPT; u++)
-                        if (!zl[u] && Rk[u] == INT_MAX) Rk[u] = lc;
+                        if (!((zl[u] >> t) & 1u) && Rk[u] == INT_MAX) Rk[u] = lc;
                 }
                 const int mt = Ee >= B ? Ee - B + 1 : 0;  // the tail scan includes column Ee
                 const int ct = (mt + NW - 1) / NW;
@@ -529,11 +612,14 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                 int Zrk = INT_MIN, Qk[LPT];
                 for (int u = 0; u < LPT; u++) Qk[u] = INT_MIN;
                 for (int lc = q0; lc > q1; lc--) {
-                    bool zl[LPT], any = false;
-                    for (int u = 0; u < LPT; u++) { zl[u] = zero_at(lc, u); any |= zl[u]; }
-                    if (!__any_sync(full, any)) { Zrk = lc; break; }
+                    unsigned zl[LPT], any = 0;
+                    for (int u = 0; u < LPT; u++) {
+                        zl[u] = liveM[u] & ~NZ[(size_t)lc * LPT + u];
+                        any |= zl[u];
+                    }
+                    if (!any) { Zrk = lc; break; }
                     for (int u = 0; u < LPT; u++)
-                        if (!zl[u] && Qk[u] == INT_MIN) Qk[u] = lc;
+                        if (!((zl[u] >> t) & 1u) && Qk[u] == INT_MIN) Qk[u] = lc;
                 }
                 for (int u = 0; u < LPT; u++) {
                     X.R[wp][t + 32 * u] = Rk[u];

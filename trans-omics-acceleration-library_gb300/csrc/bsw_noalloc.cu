@@ -49,6 +49,7 @@ void *g_scratch_dev[kMaxDevices];
 int g_num_sms[kMaxDevices];
 size_t g_smem_optin[kMaxDevices];
 bool g_ready[kMaxDevices];
+long long g_last_bad1[kMaxDevices];  // the last call's first offending pair + 1 (0: none)
 
 // Zeroes the control block (the first offending index starts at INT64_MAX).
 __global__ void noalloc_reset_kernel(NoAllocCtrl *c) {
@@ -107,6 +108,10 @@ extern "C" int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_s
         !in(p.e_ins, 1, 127) || !in(p.w_match, 0, 127) || !in(p.w_mismatch, 0, 127))
         return TAL_EINVAL;
     if (numPairs < 0 || (bits != 0 && bits != 8 && bits != 16)) return TAL_EINVAL;
+    {
+        int d = 0;
+        if (cudaGetDevice(&d) == cudaSuccess && d >= 0 && d < kMaxDevices) g_last_bad1[d] = 0;
+    }
     if (numPairs == 0) return TAL_OK;
     if (!d_pairs || !d_ref || !d_qer) return TAL_EINVAL;
     if (((uintptr_t)d_ref & 15) || ((uintptr_t)d_qer & 15)) return TAL_EINVAL;
@@ -153,13 +158,21 @@ extern "C" int tal_bsw_scores_device_noalloc(const tal_bsw_params *params, tal_s
         return TAL_ENOMEM;  // a pair too long for the shared-memory rows
     e = talbsw::launch_config(A, cfg, g_num_sms[dev], g_smem_optin[dev], s);
     if (e != cudaSuccess) return TAL_ECUDA;
-    int flags = 0;
-    e = cudaMemcpyAsync(&flags, &c->flags, sizeof(flags), cudaMemcpyDeviceToHost, s);
+    NoAllocCtrl st;
+    e = cudaMemcpyAsync(&st, c, sizeof(st), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return TAL_ECUDA;
+    const int flags = st.flags;
+    if (flags && st.bad_index != LLONG_MAX) g_last_bad1[dev] = st.bad_index + 1;
     // a pair whose rows do not fit shared memory: a capacity refusal; a pair
     // outside the exact range or with a base code above 4: a domain error
     if (flags & (talbsw::ERR_DOMAIN | talbsw::ERR_BASE)) return TAL_EDOMAIN;
     if (flags) return TAL_ENOMEM;
     return TAL_OK;
+}
+
+extern "C" int64_t tal_bsw_noalloc_last_bad_pair(void) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -1;
+    return g_last_bad1[dev] - 1;
 }

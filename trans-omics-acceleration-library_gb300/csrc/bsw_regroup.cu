@@ -272,7 +272,7 @@ __global__ void rg_reset(RegroupView V, int *err_flags, ReqDesc *reqs, int nreq)
         V.ctr[7] = V.ctr[1] + V.ctr[2];
     }
     __syncthreads();
-    if (threadIdx.x < 6) V.ctr[threadIdx.x] = 0;
+    if (threadIdx.x < 6 || (threadIdx.x >= 8 && threadIdx.x < 10)) V.ctr[threadIdx.x] = 0;
 }
 
 }  // namespace
@@ -286,23 +286,31 @@ cudaError_t RegroupBufs::ensure(long long ntotal, int cols_cap, int num_sms, boo
     while (hcap < 2 * mcap) hcap <<= 1;
     // group-kernel scratch: slots for the longer of the 16- and 8-bit rows
     const int col_cap = std::max(cols_cap, 1) + 3;
-    const long long slot_bytes = (long long)std::max(group_slot_elems(col_cap, 16), group_slot_elems(col_cap, 8)) * 2;
+    const long long slot_bytes = (long long)std::max(wide_slot_elems(col_cap, 16), wide_slot_elems(col_cap, 8)) * 2;
     // one global slot per block, for the groups whose rows do not fit shared memory
     const long long slots = std::min<long long>((long long)num_sms, std::max<long long>(4, (1LL << 30) / slot_bytes));
     if (nchunks <= V.nchunks && fcap <= V.fcap && col_cap <= V.col_cap && V.ctr) {
         return cudaSuccess;
     }
-    // the block-wide kernel: one block per group, the group's rows in shared
-    // memory up to the opt-in limit (one block per SM)
+    // the block-wide kernel, one block per group: a first launch with several
+    // blocks per SM takes the groups whose rows (a ring of the band for long
+    // queries) fit its shared memory, a second with the opt-in limit per block
+    // and a global slot per block the rest
     int dev = 0, optin = 0;
     cudaError_t e0 = cudaGetDevice(&dev);
     if (e0 == cudaSuccess) e0 = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e0 == cudaSuccess) e0 = cudaFuncSetAttribute(bsw_group_wide_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     if (e0 == cudaSuccess) e0 = cudaFuncSetAttribute(bsw_group_wide_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    const int smem1 = std::min(optin, kRegroupSmem1);
+    int bps16 = 1, bps8 = 1;
+    if (e0 == cudaSuccess)
+        e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps16, bsw_group_wide_kernel<16>, 32 * kWideWarps, smem1);
+    if (e0 == cudaSuccess)
+        e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps8, bsw_group_wide_kernel<8>, 32 * kWideWarps, smem1);
     if (e0 != cudaSuccess) return e0;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
-    const size_t o_ctr = take(sizeof(int) * 8);
+    const size_t o_ctr = take(sizeof(int) * 16);
     const size_t o_flag = take(sizeof(long long) * fcap);
     const size_t o_cls = take(sizeof(int) * fcap);
     const size_t o_gidx = take(sizeof(long long) * fcap);
@@ -346,9 +354,12 @@ cudaError_t RegroupBufs::ensure(long long ntotal, int cols_cap, int num_sms, boo
     V.hcap = (int)hcap;
     V.col_cap = col_cap;
     V.slots = (int)slots;
+    V.smem1 = smem1;
+    V.grid1[0] = num_sms * std::max(1, bps16);
+    V.grid1[1] = num_sms * std::max(1, bps8);
     V.smem = optin;
     // empty tables, zero counters (the passes leave them so)
-    if ((e = cudaMemset(V.ctr, 0, sizeof(int) * 8)) != cudaSuccess) return e;
+    if ((e = cudaMemset(V.ctr, 0, sizeof(int) * 16)) != cudaSuccess) return e;
     if ((e = cudaMemset(V.ckeys, 0xff, sizeof(unsigned long long) * kRegroupClasses)) != cudaSuccess) return e;
     if ((e = cudaMemset(V.mhash, 0xff, sizeof(unsigned long long) * hcap)) != cudaSuccess) return e;
     if ((e = cudaMemset(V.needh, 0, sizeof(unsigned long long) * hcap)) != cudaSuccess) return e;
@@ -376,7 +387,7 @@ cudaError_t enqueue_regroup(const RegroupView &V, LaunchArgs A, int nreq, long l
         G.w = A.w;
         G.bits = b == 0 ? 16 : 8;
         G.col_cap = V.col_cap;
-        G.slot_elems = group_slot_elems(V.col_cap, G.bits);
+        G.slot_elems = wide_slot_elems(V.col_cap, G.bits);
         G.scratch = V.scratch;
         G.work_counter = &V.ctr[3 + b];
         G.cells = A.cells;
@@ -390,15 +401,24 @@ cudaError_t enqueue_regroup(const RegroupView &V, LaunchArgs A, int nreq, long l
         G.ngroups_cap = V.mcap;
         G.reqs = A.reqs;
         G.nreq = nreq;
+        // first launch: the groups that fit smem1, several blocks per SM
+        G.smem_bytes = (size_t)V.smem1;
+        G.defer = true;
+        G.skip_upto = 0;
+        if (b == 0) bsw_group_wide_kernel<16><<<V.grid1[0], 32 * kWideWarps, V.smem1, s>>>(G);
+        else bsw_group_wide_kernel<8><<<V.grid1[1], 32 * kWideWarps, V.smem1, s>>>(G);
+        // second: the rest, one block per SM, global slot = block index
+        G.work_counter = &V.ctr[8 + b];
+        G.defer = false;
+        G.skip_upto = V.smem1 > (int)wide_x_bytes<kWideWarps>() ? (size_t)V.smem1 - wide_x_bytes<kWideWarps>() : 0;
         G.smem_bytes = (size_t)V.smem;
-        // one block per group at a time; a block's global slot is its index
         const int blocks = std::min(V.slots, num_sms);
         if (b == 0) bsw_group_wide_kernel<16><<<blocks, 32 * kWideWarps, V.smem, s>>>(G);
         else bsw_group_wide_kernel<8><<<blocks, 32 * kWideWarps, V.smem, s>>>(G);
     }
     rg_cleanup<<<std::max(1, num_sms), 256, 0, s>>>(V);
     rg_reset<<<1, 32, 0, s>>>(V, A.err_flags, A.reqs, nreq);
-    if (launches) *launches += 10;
+    if (launches) *launches += 11;
     return cudaGetLastError();
 }
 
