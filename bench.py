@@ -57,6 +57,9 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling)")
     ap.add_argument("--pairs", type=int, default=None,
                     help="score only the first N pairs of the workload (profiling a small case)")
+    ap.add_argument("--profile-call", action="store_true",
+                    help="profiling: warm up the batched call (--warmup calls), print the library's "
+                         "launch counter, make one more call and exit (no timing, no JSON line)")
     ap.add_argument("--no-grouped", action="store_true",
                     help="skip the grouped-form (TAL_BSW_GROUPED) leg")
     ap.add_argument("--no-extras", action="store_true", help="skip the single-shape workloads")
@@ -492,7 +495,8 @@ def run_ours(args):
                               "device time of the batched call (all its launches)"},
         "roofline_hbm": {"bound": "hbm", "achieved": round(hbm_rate, 2), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(hbm_rate / hbm_peak, 6), "peak_source": peak_src,
-                         "algorithmic_bytes_per_step": int(alg_bytes)},
+                         "algorithmic_bytes_per_step": int(alg_bytes),
+                         "traffic": profile_traffic("c3_mixed_batched")},
         "clocks": clk,
     }
     if e2e:
@@ -1024,12 +1028,45 @@ def run_reference(args):
     print(json.dumps(res), flush=True)
 
 
+def profile_call(args):
+    """One batched call of the workload after --warmup calls, for ncu: prints
+    the launch counter before the profiled call (ncu -s) and its launches (-c)."""
+    import torch
+    import tal_bsw
+    from tal_bsw import synth
+    wl = synth.WORKLOADS[args.workload]
+    n = wl.n_pairs if not args.pairs else min(args.pairs, wl.n_pairs)
+    b = synth.generate(wl, n)
+    P = wl.params()
+    bsw = tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                   P["end_bonus"], None, P["a"], P["b"], 1, device=0)
+    dp = torch.from_numpy(b.pairs.view(np.uint8).reshape(-1).copy()).cuda()
+    dr = torch.from_numpy(b.ref).cuda()
+    dq = torch.from_numpy(b.qer).cuda()
+    dw = torch.from_numpy(b.w.astype(np.int32)).cuda() if wl.w_choices else None
+    torch.cuda.synchronize()
+
+    def call():
+        bsw.scores_batched_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                                  n, wl.w, wl.bits, None if dw is None else dw.data_ptr())
+        bsw.sync()
+    for _ in range(args.warmup):
+        call()
+    l0 = bsw.launch_count
+    call()
+    print(f"launches before the profiled call: {l0}; in it: {bsw.launch_count - l0}; "
+          f"flagged pairs / groups: {bsw.last_regroup()}", flush=True)
+    bsw.close()
+
+
 def main():
     import faulthandler
     faulthandler.enable()
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.profile_call:
+        profile_call(args)
     else:
         run_ours(args)
 

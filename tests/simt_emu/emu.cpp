@@ -275,15 +275,17 @@ extern "C" int emu_bsw_group_wide_run(talbsw::DevPair *pairs, const uint8_t *ref
         G.need = need;
         G.ngroups_dev = &ng;
     }
-    const size_t xb = talbsw::wide_x_bytes<talbsw::kWideWarps>();
+    const int nw = bits == 8 ? talbsw::wide_warps<8>() : talbsw::wide_warps<16>();
+    const size_t xb = bits == 8 ? talbsw::wide_x_bytes<talbsw::wide_warps<8>()>()
+                                : talbsw::wide_x_bytes<talbsw::wide_warps<16>()>();
     G.smem_bytes = xb + (size_t)smem_rows;
     std::vector<unsigned char> smem(G.smem_bytes + 64, 0xA5);  // poisoned, like fresh smem
     auto body = [](const void *a) {
         const talbsw::GroupArgs &g = *static_cast<const talbsw::GroupArgs *>(a);
-        if (g.bits == 8) talbsw::group_wide_body<8, talbsw::kWideWarps>(g, simt::tl_smem);
-        else talbsw::group_wide_body<16, talbsw::kWideWarps>(g, simt::tl_smem);
+        if (g.bits == 8) talbsw::group_wide_body<8, talbsw::wide_warps<8>()>(g, simt::tl_smem);
+        else talbsw::group_wide_body<16, talbsw::wide_warps<16>()>(g, simt::tl_smem);
     };
-    return run_block(body, &G, talbsw::kWideWarps, smem.data());
+    return run_block(body, &G, nw, smem.data());
 }
 
 // A serving tick: nreq requests, each with its own pair array, sequence

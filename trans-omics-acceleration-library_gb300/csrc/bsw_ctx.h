@@ -124,9 +124,9 @@ struct BatchCtrl {
 // re-scored groups.
 constexpr int kRegroupClasses = 1024;  // distinct classes among one call's flagged pairs
 constexpr int kRegroupChunk = 2048;
-// Shared memory of the regroup pass's first scoring launch: up to three blocks
-// per SM, room (after the 12.5 KB of cross-warp exchange) for a 16-bit group's
-// 256-column ring (bands up to 124) with its frozen-column record up to ~5,300
+// Shared memory of the regroup pass's first scoring launch: room (after the
+// 25 KB of cross-warp exchange of a 16-warp block) for a 16-bit group's
+// 256-column ring (bands up to 124) with the lane masks of up to ~2,600
 // columns, or an 8-bit group's whole rows.
 constexpr int kRegroupSmem1 = 75 * 1024;    // pairs per counting chunk
 struct RegroupView {

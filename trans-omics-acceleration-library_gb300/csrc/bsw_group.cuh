@@ -101,7 +101,11 @@ template <int SB>
 struct GE {
     static constexpr int SH = 32 - SB;
     static constexpr unsigned MSK = (1u << SB) - 1u;
-    __device__ __forceinline__ static int ws(int x) { return (int)((unsigned)x << SH) >> SH; }
+    // the low SB bits, sign-extended (one sign-extend instruction)
+    __device__ __forceinline__ static int ws(int x) {
+        if constexpr (SB == 16) return (int)(int16_t)(uint16_t)(unsigned)x;
+        else return (int)(int8_t)(uint8_t)(unsigned)x;
+    }
     __device__ __forceinline__ static unsigned us(int x) { return (unsigned)x & MSK; }
 };
 

@@ -7,9 +7,9 @@
 // instructions per column, so a lone group (the regroup pass re-scores a few
 // hundred, spread over the device) advances one column every ~500 cycles and
 // a group of 2,000-base pairs takes tens of milliseconds.  Here NW warps
-// share the group: every warp holds all of the group's lanes (thread t of
-// each warp is lane t, and t + 32 in 8-bit), and the band is cut into NW
-// contiguous column chunks, one per warp.
+// (wide_warps) share the group: every warp holds all of the group's lanes
+// (thread t of each warp is lane t, and t + 32 in 8-bit), and the band is
+// cut into NW contiguous column chunks, one per warp.
 //
 // Per row (bandedSWA.cpp:3080-3316 for 16-bit, :2371-2621 for 8-bit):
 //  * the per-lane state (band clamp, head, tail, maxima, exit) is replicated
@@ -21,16 +21,19 @@
 //    chunk k is max(A(k-1), E(k-1) - n(k-1) * e_ins) exactly (max-plus).
 //    Pass 2: each warp re-walks its chunk from the true entering E and the
 //    previous column's H (from the neighbouring chunk's published values),
-//    storing the row exactly as the sequential walk does;
-//  * the row maximum and its last column (a packed key), the narrowing's
-//    all-zero columns and the head / tail scans are combined across warps
-//    through shared memory; each sequential scan's stopping column and each
-//    lane's first non-zero column are independent minima / maxima over the
-//    warps' parts.
+//    storing the row exactly as the sequential walk does.  Both passes load
+//    the next column's word one column ahead, and score a cell with one byte
+//    permute of the row's score table (query selectors stored per column);
+//  * every store also records the column's mask of lanes holding a non-zero
+//    word (NZ).  The narrowing reads the masks' union; the head / tail scans
+//    (each warp a part of the range) take 32 columns per step: a ballot
+//    finds the first column where no live lane is zero, a 32 x 32 bit
+//    transpose gives every lane its first column where it is not a live zero;
+//    a scan's stopping column and each lane's first such column are minima /
+//    maxima over the warps' parts, combined through shared memory, as are
+//    the row maximum with its last column (a packed key).
 // Every value is kept in the element width and wraps as the reference's
-// does, as in bsw_group.cuh.  The group's rows (H and F packed in one word,
-// the query codes) are in shared memory when they fit, else in the block's
-// slot of global scratch.
+// does, as in bsw_group.cuh.
 //
 // Member mode stops a group once its needed lanes (the flagged pairs) have
 // exited: a lane's outputs freeze at its exit, and only the needed lanes'
@@ -44,7 +47,10 @@
 
 namespace talbsw {
 
-constexpr int kWideWarps = 8;  // warps per group (4 measured 6.2 against 3.2 ms for C2's regroup pass)
+// Warps per group: 16 for 16-bit groups (4 / 8 / 16 measured 6.2 / 3.2 / 2.6 ms for
+// C2's regroup pass), 8 for 8-bit ones (two lanes per thread need ~160 registers)
+template <int SB>
+__host__ __device__ constexpr int wide_warps() { return SB == 16 ? 16 : 8; }
 
 // Cross-warp exchange of one block, at the start of its shared memory.
 template <int NW>
@@ -61,6 +67,18 @@ struct WideX {
     int R[NW][64], Q[NW][64];  // head / tail scan: a lane's first / last non-zero column
     int gscore[64], max_ie[64];
 };
+
+// 32 x 32 bit transpose across a warp: thread t holds row t on entry and
+// column t on return (bit r of the result = bit t of thread r's row), in
+// five exchange steps of halving width (the recursive block transpose).
+__device__ __forceinline__ unsigned transpose32(unsigned x, int t) {
+    unsigned m = 0x0000ffffu;
+    for (int j = 16; j != 0; j >>= 1, m ^= (m << j)) {
+        const unsigned y = __shfl_xor_sync(0xffffffffu, x, j);
+        x = (t & j) ? (((y >> j) & m) | (x & ~m)) : ((x & m) | ((y << j) & ~m));
+    }
+    return x;
+}
 
 template <int NW>
 __host__ __device__ constexpr size_t wide_x_bytes() {
@@ -267,29 +285,29 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
             HF = HFg;
         }
         const int wm = WR - 1;
-        int8_t *const Q2 = reinterpret_cast<int8_t *>(HF + (size_t)WR * W);
+        // query selectors: one byte per lane and slot, [slot][lane] like HF
+        uint8_t *const Q2 = reinterpret_cast<uint8_t *>(HF + (size_t)WR * W);
         uint32_t *const NZ = reinterpret_cast<uint32_t *>(
             reinterpret_cast<uintptr_t>(Q2 + ((((size_t)WR + 3) & ~(size_t)3) + 8) * W + 15) & ~(uintptr_t)15);
         auto slot = [&](int c) -> int { return ring ? (c & wm) : c; };
         auto HFa = [&](int c, int u) -> uint32_t & { return HF[(size_t)slot(c) * W + t + 32 * u]; };
-        auto code_at = [&](int c, int u) -> int {
-            const int sc = slot(c);
-            return Q2[(((size_t)(sc >> 2) * W + t + 32 * u) << 2) + (sc & 3)];
-        };
         auto pack = [](int h, int f) -> uint32_t { return (uint32_t)(uint16_t)h | ((uint32_t)(uint16_t)f << 16); };
-        // column k's query code and row-0 entry, for every lane of this thread
+        // column k's query selector and row-0 entry, for every lane of this
+        // thread.  Selector: 0 for N, 1 + b for base b, 5 for the padding code
+        // past the lane's query (DUMMY2, :46) -- the byte of the row's score
+        // table (below) that holds S(target base, query code)
         auto init_col = [&](int k) {
             const int sc = slot(k);
             for (int u = 0; u < LPT; u++) {
                 const int l = t + 32 * u;
-                int code = 0;
+                int sel = 1;
                 if (k < len2[u]) {
                     const int b = qp[u] ? qp[u][k] : 4;
-                    code = b == 4 ? -1 : E::ws(b);
+                    sel = b == 4 ? 0 : b + 1;
                 } else if (k <= maxLen2) {
-                    code = 100;  // DUMMY2 (:46)
+                    sel = 5;
                 }
-                Q2[(((size_t)(sc >> 2) * W + l) << 2) + (sc & 3)] = (int8_t)code;
+                Q2[(size_t)sc * W + l] = (uint8_t)sel;
                 int hv = 0;
                 if (k == 0) hv = h0[u];
                 else if (k == 1) hv = tt1[u];
@@ -329,6 +347,7 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
         for (int i = 0; i < nrow; i++) {
             const int i1 = E::ws(i + 1);
             int h10[LPT], maxRS1[LPT], y1[LPT], s1[LPT];
+            uint32_t tlo[LPT], thi[LPT];  // the row's score table (bytes by selector)
             beg = nbeg; end = nend;
             if (beg < i - w) beg = i - w;
             if (end > i + w + 1) end = i + w + 1;
@@ -344,6 +363,19 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                     if (b > 4) gerr(ERR_BASE, lidx[u]);
                 } else {
                     s1[u] = 99;  // DUMMY1
+                }
+                // score of the row's target code s1 against each query
+                // selector, as the kernel's blends compute it (:1883-1906): match
+                // or mismatch, -1 where either side is N (negative code)
+                {
+                    const uint32_t mt = (uint32_t)(uint8_t)w_match, ms = (uint32_t)(uint8_t)w_mismatch;
+                    uint32_t lo = 0xffu | (ms << 8) | (ms << 16) | (ms << 24);  // N, bases 0..2
+                    uint32_t hi = ms | (ms << 8) | (ms << 16) | (ms << 24);     // base 3, DUMMY2, -
+                    if (s1[u] >= 0 && s1[u] <= 2) lo = (lo & ~(0xffu << (8 * (s1[u] + 1)))) | (mt << (8 * (s1[u] + 1)));
+                    else if (s1[u] == 3) hi = (hi & ~0xffu) | mt;
+                    if (s1[u] < 0) { lo = 0xffffffffu; hi = 0xffffffffu; }
+                    tlo[u] = lo;
+                    thi[u] = hi;
                 }
                 // per-lane band (:3080-3089)
                 const int ph = head[u], pt = tail[u];
@@ -393,9 +425,8 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
             const int n = end > beg ? end - beg : 0;
             const int cs = (n + NW - 1) / NW;
             const int c0 = beg + imin(n, wp * cs), c1 = beg + imin(n, (wp + 1) * cs);
-            auto m11_of = [&](int a2, int u, int h00) -> int {
-                int sbt = s1[u] == a2 ? w_match : w_mismatch;
-                if ((s1[u] | a2) < 0) sbt = -1;  // an N on either side
+            auto m11_of = [&](uint32_t sel, int u, int h00) -> int {
+                const int sbt = (int)(int8_t)(uint8_t)__byte_perm(tlo[u], thi[u], sel);
                 const int m11 = E::ws(h00 + sbt);
                 return h00 == 0 ? 0 : m11;
             };
@@ -404,14 +435,17 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
             if (c1 > c0) {
                 for (int u = 0; u < LPT; u++) {
                     int el = 0;
-                    uint32_t hfn = HFa(c0, u);
-                    int an = code_at(c0, u);
+                    int bi = slot(c0) * W + t + 32 * u;  // element of (column j, lane)
+                    uint32_t hfn = HF[bi];
+                    uint32_t an = Q2[bi];
                     for (int j = c0; j < c1; j++) {
                         const uint32_t hf = hfn;
-                        const int a2 = an;
+                        const uint32_t a2 = an;
+                        bi += W;
+                        if (ring && bi >= WR * W) bi -= WR * W;
                         if (j + 1 < c1) {
-                            hfn = HFa(j + 1, u);
-                            an = code_at(j + 1, u);
+                            hfn = HF[bi];
+                            an = Q2[bi];
                         }
                         const int h00 = (int16_t)(hf & 0xffffu), f11 = (int16_t)(hf >> 16);
                         const int m11 = m11_of(a2, u, h00);
@@ -445,23 +479,29 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                         h10[u] = imax(X.MF[wp - 1][l], el);
                     }
                 }
-                uint32_t hfn[LPT];
-                int an[LPT];
+                uint32_t hfn[LPT], an[LPT];
+                int gcol[LPT];  // the query's last column, where gscore is taken (:3178-3195)
+                int bj = slot(c0) * W + t;  // element of (column j, lane t)
                 for (int u = 0; u < LPT; u++) {
-                    hfn[u] = HFa(c0, u);
-                    an[u] = code_at(c0, u);
+                    hfn[u] = HF[bj + 32 * u];
+                    an[u] = Q2[bj + 32 * u];
+                    gcol[u] = qlen[u] - 1 >= minq ? qlen[u] - 1 : -1;
                 }
                 for (int j = c0; j < c1; j++) {
-                    const int pj = E::ws(j);
-                    const int jn = E::ws(j + 1);
+                    // j + 1 <= ncol fits the element width: no wrap
+                    const int pj = j;
+                    const int jn = j + 1;
+                    const int bc = bj;
+                    bj += W;
+                    if (ring && bj >= WR * W) bj -= WR * W;
                     unsigned nzc = 0;
                     for (int u = 0; u < LPT; u++) {
                         const int l = t + 32 * u;
                         const uint32_t hf = hfn[u];
-                        const int a2 = an[u];
+                        const uint32_t a2 = an[u];
                         if (j + 1 < c1) {  // next column's inputs (never this column's store)
-                            hfn[u] = HFa(j + 1, u);
-                            an[u] = code_at(j + 1, u);
+                            hfn[u] = HF[bj + 32 * u];
+                            an[u] = Q2[bj + 32 * u];
                         }
                         const int h00 = (int16_t)(hf & 0xffffu), f11 = (int16_t)(hf >> 16);
                         const int m11 = m11_of(a2, u, h00);
@@ -487,14 +527,13 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                             maxRS1[u] = nm;
                         }
                         const uint32_t word = pack(hst, f21);
-                        HFa(j, u) = word;
+                        HF[bc + 32 * u] = word;
                         const unsigned m = __ballot_sync(full, word != 0u);
                         if (t == 0) NZ[(size_t)j * LPT + u] = m;
                         nzc |= m;
                         h10[u] = h11;
                         // end-to-end score (:3178-3195), in the query's last column
-                        if (j >= minq && jn == qlen[u] && exit0[u] < 0 && !(jn > tail[u]) &&
-                            !(X.gscore[l] > h11)) {
+                        if (j == gcol[u] && exit0[u] < 0 && !(jn > tail[u]) && !(X.gscore[l] > h11)) {
                             X.gscore[l] = h11;
                             X.max_ie[l] = i1;
                         }
@@ -594,32 +633,50 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                 const int mh = Ee > B ? Ee - B : 0;
                 const int ch = (mh + NW - 1) / NW;
                 const int p0 = B + imin(mh, wp * ch), p1 = B + imin(mh, (wp + 1) * ch);
+                // 32 columns per step, thread t holding column cb + t (head scan)
+                // or ct - t (tail scan, downwards): a ballot gives the columns
+                // where no live lane is zero, and a bit transpose gives each
+                // lane (thread) the columns where it is not a live zero
                 int Zk = INT_MAX, Rk[LPT];
                 for (int u = 0; u < LPT; u++) Rk[u] = INT_MAX;
-                for (int lc = p0; lc < p1; lc++) {
-                    unsigned zl[LPT], any = 0;  // live lanes holding a zero word at lc
+                for (int cb = p0; cb < p1; cb += 32) {
+                    const int c = cb + t;
+                    const bool inr = c < p1;
+                    unsigned zlive = 0;
+                    unsigned ok[LPT];  // lanes that are not a live zero at column c
                     for (int u = 0; u < LPT; u++) {
-                        zl[u] = liveM[u] & ~NZ[(size_t)lc * LPT + u];
-                        any |= zl[u];
+                        const unsigned nz = inr ? NZ[(size_t)c * LPT + u] : 0u;
+                        zlive |= liveM[u] & ~nz;
+                        ok[u] = inr ? (~liveM[u] | nz) : 0u;
                     }
-                    if (!any) { Zk = lc; break; }
-                    for (int u = 0; u < LPT; u++)
-                        if (!((zl[u] >> t) & 1u) && Rk[u] == INT_MAX) Rk[u] = lc;
+                    const unsigned zc = __ballot_sync(full, inr && zlive == 0u);
+                    for (int u = 0; u < LPT; u++) {
+                        const unsigned x = transpose32(ok[u], t);
+                        if (Rk[u] == INT_MAX && x) Rk[u] = cb + __ffs(x) - 1;
+                    }
+                    if (zc) { Zk = cb + __ffs(zc) - 1; break; }
                 }
                 const int mt = Ee >= B ? Ee - B + 1 : 0;  // the tail scan includes column Ee
                 const int ct = (mt + NW - 1) / NW;
                 const int q0 = Ee - imin(mt, wp * ct), q1 = Ee - imin(mt, (wp + 1) * ct);
                 int Zrk = INT_MIN, Qk[LPT];
                 for (int u = 0; u < LPT; u++) Qk[u] = INT_MIN;
-                for (int lc = q0; lc > q1; lc--) {
-                    unsigned zl[LPT], any = 0;
+                for (int cb = q0; cb > q1; cb -= 32) {
+                    const int c = cb - t;
+                    const bool inr = c > q1;
+                    unsigned zlive = 0;
+                    unsigned ok[LPT];
                     for (int u = 0; u < LPT; u++) {
-                        zl[u] = liveM[u] & ~NZ[(size_t)lc * LPT + u];
-                        any |= zl[u];
+                        const unsigned nz = inr ? NZ[(size_t)c * LPT + u] : 0u;
+                        zlive |= liveM[u] & ~nz;
+                        ok[u] = inr ? (~liveM[u] | nz) : 0u;
                     }
-                    if (!any) { Zrk = lc; break; }
-                    for (int u = 0; u < LPT; u++)
-                        if (!((zl[u] >> t) & 1u) && Qk[u] == INT_MIN) Qk[u] = lc;
+                    const unsigned zc = __ballot_sync(full, inr && zlive == 0u);
+                    for (int u = 0; u < LPT; u++) {
+                        const unsigned x = transpose32(ok[u], t);
+                        if (Qk[u] == INT_MIN && x) Qk[u] = cb - (__ffs(x) - 1);
+                    }
+                    if (zc) { Zrk = cb - (__ffs(zc) - 1); break; }
                 }
                 for (int u = 0; u < LPT; u++) {
                     X.R[wp][t + 32 * u] = Rk[u];
@@ -676,9 +733,9 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
 }
 
 template <int SB>
-__global__ void __launch_bounds__(32 * kWideWarps, 1) bsw_group_wide_kernel(GroupArgs A) {
+__global__ void __launch_bounds__(32 * wide_warps<SB>(), 1) bsw_group_wide_kernel(GroupArgs A) {
     TALBSW_DYNAMIC_SMEM(smem_w);
-    group_wide_body<SB, kWideWarps>(A, smem_w);
+    group_wide_body<SB, wide_warps<SB>()>(A, smem_w);
 }
 
 }  // namespace talbsw

@@ -304,9 +304,9 @@ cudaError_t RegroupBufs::ensure(long long ntotal, int cols_cap, int num_sms, boo
     const int smem1 = std::min(optin, kRegroupSmem1);
     int bps16 = 1, bps8 = 1;
     if (e0 == cudaSuccess)
-        e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps16, bsw_group_wide_kernel<16>, 32 * kWideWarps, smem1);
+        e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps16, bsw_group_wide_kernel<16>, 32 * wide_warps<16>(), smem1);
     if (e0 == cudaSuccess)
-        e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps8, bsw_group_wide_kernel<8>, 32 * kWideWarps, smem1);
+        e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps8, bsw_group_wide_kernel<8>, 32 * wide_warps<8>(), smem1);
     if (e0 != cudaSuccess) return e0;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
@@ -405,16 +405,17 @@ cudaError_t enqueue_regroup(const RegroupView &V, LaunchArgs A, int nreq, long l
         G.smem_bytes = (size_t)V.smem1;
         G.defer = true;
         G.skip_upto = 0;
-        if (b == 0) bsw_group_wide_kernel<16><<<V.grid1[0], 32 * kWideWarps, V.smem1, s>>>(G);
-        else bsw_group_wide_kernel<8><<<V.grid1[1], 32 * kWideWarps, V.smem1, s>>>(G);
+        if (b == 0) bsw_group_wide_kernel<16><<<V.grid1[0], 32 * wide_warps<16>(), V.smem1, s>>>(G);
+        else bsw_group_wide_kernel<8><<<V.grid1[1], 32 * wide_warps<8>(), V.smem1, s>>>(G);
         // second: the rest, one block per SM, global slot = block index
         G.work_counter = &V.ctr[8 + b];
         G.defer = false;
-        G.skip_upto = V.smem1 > (int)wide_x_bytes<kWideWarps>() ? (size_t)V.smem1 - wide_x_bytes<kWideWarps>() : 0;
+        const size_t xb = b == 0 ? wide_x_bytes<wide_warps<16>()>() : wide_x_bytes<wide_warps<8>()>();
+        G.skip_upto = (size_t)V.smem1 > xb ? (size_t)V.smem1 - xb : 0;
         G.smem_bytes = (size_t)V.smem;
         const int blocks = std::min(V.slots, num_sms);
-        if (b == 0) bsw_group_wide_kernel<16><<<blocks, 32 * kWideWarps, V.smem, s>>>(G);
-        else bsw_group_wide_kernel<8><<<blocks, 32 * kWideWarps, V.smem, s>>>(G);
+        if (b == 0) bsw_group_wide_kernel<16><<<blocks, 32 * wide_warps<16>(), V.smem, s>>>(G);
+        else bsw_group_wide_kernel<8><<<blocks, 32 * wide_warps<8>(), V.smem, s>>>(G);
     }
     rg_cleanup<<<std::max(1, num_sms), 256, 0, s>>>(V);
     rg_reset<<<1, 32, 0, s>>>(V, A.err_flags, A.reqs, nreq);
