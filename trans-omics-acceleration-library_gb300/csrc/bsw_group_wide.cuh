@@ -296,13 +296,17 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
         // thread.  Selector: 0 for N, 1 + b for base b, 5 for the padding code
         // past the lane's query (DUMMY2, :46) -- the byte of the row's score
         // table (below) that holds S(target base, query code)
+        // warp wp initialises the columns k = wp mod NW and loads the query
+        // byte of its next one a row ahead (kp, bp), off the row's critical path
+        int kp = -1, bp[LPT];
+        auto qbyte = [&](int k, int u) -> int { return k < len2[u] && qp[u] ? qp[u][k] : 4; };
         auto init_col = [&](int k) {
             const int sc = slot(k);
             for (int u = 0; u < LPT; u++) {
                 const int l = t + 32 * u;
                 int sel = 1;
                 if (k < len2[u]) {
-                    const int b = qp[u] ? qp[u][k] : 4;
+                    const int b = k == kp ? bp[u] : qbyte(k, u);
                     sel = b == 4 ? 0 : b + 1;
                 } else if (k <= maxLen2) {
                     sel = 5;
@@ -393,8 +397,13 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
             const int lim = imin(colCap - 1, i + w + 3);
             const bool ini = initc <= lim;
             if (ini) {
-                for (int k = initc + wp; k <= lim; k += NW) init_col(k);
+                for (int k = initc + ((wp - initc) & (NW - 1)); k <= lim; k += NW) init_col(k);
                 initc = lim + 1;
+                const int kn = initc + ((wp - initc) & (NW - 1));
+                if (kn < colCap && kn != kp) {
+                    kp = kn;
+                    for (int u = 0; u < LPT; u++) bp[u] = qbyte(kn, u);
+                }
             }
             // trimming (:3091-3112): the sequential pass stops at the first
             // column no lane's head is beyond, so it covers [beg, max head)
