@@ -117,8 +117,10 @@ int tal_bsw_destroy(tal_bsw_handle h);
  * used where the pair is inside them), and no outputs are written.
  * Capacity: a pair's rows live in shared memory, as a ring of the band's
  * columns (2w + 12 up to 16,384, any query length) or as whole rows (queries
- * up to ~22,000 bases); a call whose pairs fit neither (a query above
- * ~22,000 bases with w above 8,186) also gives TAL_EDOMAIN. */
+ * up to ~22,000 bases); a pair that fits neither (a query above ~22,000
+ * bases with w above 8,186) is scored with the flagged pairs' groups, its
+ * rows in global memory (slowly: ~seconds for a 30,000-base query with a
+ * band of 20,000).  With TAL_BSW_PER_PAIR such a pair gives TAL_EDOMAIN. */
 int tal_bsw_scores(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t *seqBufRef,
                    const uint8_t *seqBufQer, int32_t numPairs, int32_t w, int bits);
 

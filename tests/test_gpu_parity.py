@@ -173,7 +173,8 @@ def test_long_queries_near_the_16_bit_limit():
     a band of 8,000 in a 16,384-column ring (G lanes per pair), a band of
     10,000 in whole rows of 22,000 columns, and each in the grouped kernel; a
     query of 30,000 with a band of 20,000 needs more shared memory than a
-    block has for the per-pair kernels: TAL_EDOMAIN."""
+    block has for the per-pair kernels: the regroup pass scores it exactly
+    (TAL_EDOMAIN with per-pair semantics)."""
     from _cases import DEFAULT, pack
     rng = np.random.default_rng(77)
 
@@ -193,11 +194,20 @@ def test_long_queries_near_the_16_bit_limit():
         # the grouped kernel keeps its rows in global scratch: same outputs
         got = _gpu(p, r, q, w, DEFAULT, 16 | tal_bsw.api.GROUPED)
         _assert_same(exp, got, f"long queries, w={w}, grouped")
-    refs, qers = zip(*[pair(30000, 0)])
-    p, r, q = pack(list(refs), list(qers), [50])
+    # rows too long for shared memory: exact through the regroup pass (rows in
+    # global scratch); with per-pair semantics a refusal.  The target follows the
+    # query for 3,000 bases and then diverges, so the alignment ends by z-drop
+    # and the re-scored group stops early
+    r0, q0 = pair(30000, 0)
+    r0[3000:] = rng.integers(0, 4, r0.shape[0] - 3000).astype(np.uint8)
+    refs, qers = zip(*[(r0, q0), pair(600, 20)])
+    p, r, q = pack(list(refs), list(qers), [50, 50])
+    exp = oracle.vector(p, r, q, 20000, DEFAULT, bits=16)
+    got = _gpu(p, r, q, 20000, DEFAULT, 16)
+    _assert_same(exp, got, "a query of 30,000 with a band of 20,000")
     with _bsw(DEFAULT) as bsw:
         with pytest.raises(tal_bsw.TalBswError) as ei:
-            bsw.getScores16(p.copy(), r, q, 1, 1, 20000)
+            bsw._scores(p.copy(), r, q, 2, 20000, 16 | tal_bsw.api.PER_PAIR)
         assert ei.value.status == tal_bsw.api.TAL_EDOMAIN
 
 

@@ -120,10 +120,21 @@ int launch_scoring(tal_bsw_ctx *h, talbsw::LaunchArgs A, int w_for_k, int slot =
     A.P = h->kp;
     // one band for every pair: the lane kernel keeps a ring of columns
     A.win = A.wpair ? 0 : talbsw::lane_window(A.w, A.cols_cap);
-    const talbsw::KConfig cfg = talbsw::fit_config(talbsw::choose_config(w_for_k, A.cols_cap, A.win),
-                                                   A.cols_cap, h->smem_optin, A.win);
-    if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap, A.win) > h->smem_optin)
-        return fail(h, TAL_EDOMAIN, "pair too long for the shared-memory row buffers");
+    talbsw::KConfig cfg = talbsw::fit_config(talbsw::choose_config(w_for_k, A.cols_cap, A.win),
+                                             A.cols_cap, h->smem_optin, A.win);
+    if (talbsw::config_smem(cfg, A.cols_cap, A.rows_cap, A.win) > h->smem_optin) {
+        if (!A.flagged) return fail(h, TAL_EDOMAIN, "pair too long for the shared-memory row buffers");
+        // exact mode: the per-pair kernels take the pairs whose rows fit and
+        // flag the longer ones, whose groups the regroup pass scores (rows in
+        // global scratch)
+        int cc = A.cols_cap;
+        do {
+            cc = cc > 1056 ? cc - 512 : cc / 2;
+            A.win = A.wpair ? 0 : talbsw::lane_window(A.w, cc);
+            cfg = talbsw::fit_config(talbsw::choose_config(w_for_k, cc, A.win), cc, h->smem_optin, A.win);
+        } while (cc > 32 && talbsw::config_smem(cfg, cc, A.rows_cap, A.win) > h->smem_optin);
+        A.cols_cap = cc;
+    }
     Ctrl init = {0, 0, (long long)INT64_MAX, 0ull};
     cudaError_t e = cudaMemcpyAsync(c, &init, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(ctrl)");
