@@ -60,6 +60,8 @@ def parse_args():
     ap.add_argument("--profile-call", action="store_true",
                     help="profiling: warm up the batched call (--warmup calls), print the library's "
                          "launch counter, make one more call and exit (no timing, no JSON line)")
+    ap.add_argument("--profile-plain", action="store_true",
+                    help="with --profile-call: the plain launch (tal_bsw_scores_device) instead of the batched form")
     ap.add_argument("--no-grouped", action="store_true",
                     help="skip the grouped-form (TAL_BSW_GROUPED) leg")
     ap.add_argument("--no-extras", action="store_true", help="skip the single-shape workloads")
@@ -754,6 +756,11 @@ def run_serving(args, dist, peak_pairs_per_s):
             "p50_ms": round(float(np.percentile(lat, 50)) / 1e6, 3),
             "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3),
             "max_ms": round(float(lat.max()) / 1e6, 3),
+            # the queueing-free floor: the largest request's service time at the
+            # batched rate (the whole GPU), and with processor sharing at this load
+            "p99_floor_ms": {"largest_request_at_batched_rate": round(float(sizes.max()) / peak_pairs_per_s * 1e3, 3),
+                             "same_under_processor_sharing": round(float(sizes.max()) / peak_pairs_per_s * 1e3
+                                                                   / max(1.0 - load, 1e-3), 3)},
             "mean_tick_requests": round(float(np.mean(ticks)), 2),
             "mean_ms": {"submit_to_admit": round(float(stage[:, 0].mean()), 3),
                         "admit_to_launch": round(float(stage[:, 1].mean()), 3),
@@ -1047,8 +1054,12 @@ def profile_call(args):
     torch.cuda.synchronize()
 
     def call():
-        bsw.scores_batched_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
-                                  n, wl.w, wl.bits, None if dw is None else dw.data_ptr())
+        if args.profile_plain:
+            bsw.scores_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                              n, wl.w, wl.bits, None if dw is None else dw.data_ptr())
+        else:
+            bsw.scores_batched_device(dp.data_ptr(), dr.data_ptr(), dr.numel(), dq.data_ptr(), dq.numel(),
+                                      n, wl.w, wl.bits, None if dw is None else dw.data_ptr())
         bsw.sync()
     for _ in range(args.warmup):
         call()

@@ -339,16 +339,10 @@ __global__ void __launch_bounds__(128, SB == 16 ? 12 : 5) bsw_group_kernel(Group
                 if ((s1[u] | a2) < 0) sbt = -1;
                 int m11 = E::ws(h00 + sbt);
                 if (h00 == 0) m11 = 0;
-                int h11 = m11 > e11[u] ? m11 : e11[u];
-                h11 = h11 > f11 ? h11 : f11;
-                int tv = E::ws(m11 - oe_ins);
-                int val = tv > 0 ? tv : 0;
-                const int ee = E::ws(e11[u] - e_ins);
-                e11[u] = val > ee ? val : ee;
-                tv = E::ws(m11 - oe_del);
-                val = tv > 0 ? tv : 0;
-                int f21 = E::ws(f11 - e_del);
-                f21 = val > f21 ? val : f21;
+                const int h11 = __vimax3_s32(m11, e11[u], f11);
+                // E and F are >= 0 throughout: E - e_ins, F - e_del cannot wrap
+                e11[u] = __vimax3_s32(E::ws(m11 - oe_ins), 0, e11[u] - e_ins);
+                int f21 = __vimax3_s32(E::ws(m11 - oe_del), 0, f11 - e_del);
                 const bool cmp2 = head[u] > pj;
                 const bool mask = pj > tail[u] || cmp2;
                 const int hst = mask ? 0 : h10[u];

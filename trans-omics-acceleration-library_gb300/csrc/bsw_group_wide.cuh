@@ -351,6 +351,7 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
         for (int i = 0; i < nrow; i++) {
             const int i1 = E::ws(i + 1);
             int h10[LPT], maxRS1[LPT], y1[LPT], s1[LPT];
+            unsigned rkey[LPT];  // this warp's chunk: row maximum key
             uint32_t tlo[LPT], thi[LPT];  // the row's score table (bytes by selector)
             beg = nbeg; end = nend;
             if (beg < i - w) beg = i - w;
@@ -358,7 +359,7 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
             if (end > ncol) end = ncol;
             bool changed = false;
             for (int u = 0; u < LPT; u++) {
-                maxRS1[u] = 0; y1[u] = 0;
+                maxRS1[u] = 0; y1[u] = 0; rkey[u] = 0;
                 h10[u] = beg == 0 ? Hv(i + 1, u) : 0;
                 if (i < len1[u]) {
                     const int b = tnext[u];  // loaded a row ahead
@@ -462,10 +463,8 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                             X.Elast[wp][t + 32 * u] = el;
                             X.MF[wp][t + 32 * u] = imax(m11, f11);
                         }
-                        const int tv = E::ws(m11 - oe_ins);
-                        const int val = tv > 0 ? tv : 0;
-                        const int ee = E::ws(el - e_ins);
-                        el = val > ee ? val : ee;
+                        // E >= 0 throughout, so E - e_ins cannot wrap
+                        el = __vimax3_s32(E::ws(m11 - oe_ins), 0, el - e_ins);
                     }
                     X.Aagg[wp][t + 32 * u] = el;
                 }
@@ -514,27 +513,19 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                         }
                         const int h00 = (int16_t)(hf & 0xffffu), f11 = (int16_t)(hf >> 16);
                         const int m11 = m11_of(a2, u, h00);
-                        int h11 = m11 > e11[u] ? m11 : e11[u];
-                        h11 = h11 > f11 ? h11 : f11;
-                        int tv = E::ws(m11 - oe_ins);
-                        int val = tv > 0 ? tv : 0;
-                        const int ee = E::ws(e11[u] - e_ins);
-                        e11[u] = val > ee ? val : ee;
-                        tv = E::ws(m11 - oe_del);
-                        val = tv > 0 ? tv : 0;
-                        int f21 = E::ws(f11 - e_del);
-                        f21 = val > f21 ? val : f21;
+                        const int h11 = __vimax3_s32(m11, e11[u], f11);
+                        // E and F are >= 0 throughout: E - e_ins, F - e_del cannot wrap
+                        e11[u] = __vimax3_s32(E::ws(m11 - oe_ins), 0, e11[u] - e_ins);
+                        int f21 = __vimax3_s32(E::ws(m11 - oe_del), 0, f11 - e_del);
                         const bool cmp2 = head[u] > pj;
                         const bool mask = pj > tail[u] || cmp2;
                         const int hst = mask ? 0 : h10[u];
                         if (mask) f21 = 0;
-                        const int bmax = maxRS1[u];
-                        const int nm = maxRS1[u] > h11 ? maxRS1[u] : h11;
-                        const bool cmpA = nm > bmax || nm == h11;
-                        if (!(jn > tail[u] || cmp2)) {
-                            if (cmpA) y1[u] = jn;
-                            maxRS1[u] = nm;
-                        }
+                        // the row maximum and the last column attaining it, as one key
+                        // (h11 >= 0 and jn < 2^16: the larger key is the later column of
+                        // a tie, as the sequential walk's >= keeps)
+                        const unsigned kc = ((unsigned)h11 << 16) | (unsigned)jn;
+                        if (!(jn > tail[u] || cmp2)) rkey[u] = kc > rkey[u] ? kc : rkey[u];
                         const uint32_t word = pack(hst, f21);
                         HF[bc + 32 * u] = word;
                         const unsigned m = __ballot_sync(full, word != 0u);
@@ -554,7 +545,7 @@ __device__ __forceinline__ void group_wide_body(const GroupArgs &A, unsigned cha
                 }
             }
             for (int u = 0; u < LPT; u++)
-                X.key[wp][t + 32 * u] = ((unsigned)maxRS1[u] << 16) | (unsigned)y1[u];
+                X.key[wp][t + 32 * u] = rkey[u];
             if (t == 0) {
                 X.nzF[wp] = fnz;
                 X.nzL[wp] = lnz;

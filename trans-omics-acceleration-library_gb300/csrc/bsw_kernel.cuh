@@ -757,9 +757,14 @@ __global__ void __launch_bounds__(128, 5) bsw_kernel(LaunchArgs A) {
             // entries a group may trim [beg, th) when the lane does not
             const int th = stay ? imax(ps.cp.trim_hi(changed, end, ps.head), beg) : beg;
             const int a = rowact ? imin(ps.cp.frozenTo, beg) : 0;
-            int fmin, fmax;
-            bool tnz;
-            scan_frozen_trim<G>(Hh, Fv, a, beg, th, rowact, gl, gshift, gbits, wm, fmin, fmax, tnz);
+            // the usual row: one column froze and no old entry is in question --
+            // read it directly; otherwise the ballot pass over [a, th)
+            const bool one = rowact && th <= beg && beg - a <= 1;
+            int fmin = 1 << 30, fmax = -1, smin, smax;
+            bool tnz = false, stnz;
+            if (one && beg - a == 1 && (Hh[(beg - 1) & wm] | Fv[(beg - 1) & wm]) != 0) fmin = fmax = beg - 1;
+            scan_frozen_trim<G>(Hh, Fv, a, beg, th, rowact && !one, gl, gshift, gbits, wm, smin, smax, stnz);
+            if (!one) { fmin = smin; fmax = smax; tnz = stnz; }
             if (rowact) {
                 if (fmax >= 0) { ps.cp.frozen_nz(fmin); ps.cp.frozen_nz(fmax); }
                 ps.cp.frozenTo = imax(ps.cp.frozenTo, beg);
