@@ -12,7 +12,7 @@ import tal_bsw
 from tal_bsw import synth
 from tal_bsw.seqpair import outputs
 
-from _cases import edge_cases, workload_slices
+from _cases import DEFAULT, edge_cases, extension_pairs, workload_slices
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -331,6 +331,63 @@ def test_server_is_exact_on_coupled_requests():
     for (p, _, _, _, _, e), info, name in zip(reqs, infos, range(len(reqs))):
         assert info is not None and info.status == tal_bsw.api.TAL_OK
         _assert_same(e, p, f"server request {name}")
+
+
+def _extension_batch(w):
+    """About 14,000 right-extension pairs of 6,000 reads (queries 100-250 bp
+    after the seed), in seed order, band w."""
+    return extension_pairs(6000, w, 100, 250, 1000 + w, DEFAULT)
+
+
+@pytest.mark.parametrize("w", [4, 8, 16])
+def test_default_path_is_exact_on_extension_batches(w):
+    """Stress of the default (exact) path at scale: whole seed-extension
+    batches with narrow bands, where tens of pairs per batch have outputs
+    that depend on their SIMD group.  The plain call equals the reference's
+    grouped outputs on every pair, 16-bit on the whole batch and 8-bit on
+    its int8-eligible pairs."""
+    pairs, ref, qer = _extension_batch(w)
+    for bits, sel in ((16, np.arange(pairs.shape[0])),
+                      (8, np.nonzero(oracle.eligible8(pairs, w, DEFAULT))[0])):
+        p = pairs[sel]
+        exp = oracle.vector(p, ref, qer, w, DEFAULT, bits=bits, nthreads=8)
+        alone = oracle.vector(p, ref, qer, w, DEFAULT, bits=bits, lanes=1, nthreads=8)
+        coupled = int((outputs(alone) != outputs(exp)).any(1).sum())
+        assert coupled >= 1, "the batch should hold group-dependent pairs"
+        with _bsw(DEFAULT) as bsw:
+            got = p.copy()
+            bsw._scores(got, ref, qer, got.shape[0], w, bits)
+            flagged, groups = bsw.last_regroup()
+        _assert_same(exp, got, f"extension batch w={w} bits={bits} ({coupled} group-dependent pairs)")
+        assert flagged >= 1 and groups >= 1
+
+
+def test_batched_form_is_exact_on_mixed_extension_batches():
+    """The batched form on the three extension batches mixed (bands 4, 8 and
+    16 per pair, 8/16-bit routing per pair, interleaved in runs of 11): equal
+    to the reference's caller splitting the batch into one call per (band,
+    precision) class, pairs in array order."""
+    rows, refs, qers, ws = [], [], [], []
+    roff = qoff = 0
+    for w in (4, 8, 16):
+        p, r, q = _extension_batch(w)
+        p = p.copy()
+        p["idr"] += roff
+        p["idq"] += qoff
+        rows.append(p); refs.append(r); qers.append(q); ws.append(np.full(p.shape[0], w, np.int32))
+        roff += r.shape[0]; qoff += q.shape[0]
+    pairs, wpair = np.concatenate(rows), np.concatenate(ws)
+    ref, qer = np.concatenate(refs), np.concatenate(qers)
+    runs = np.array_split(np.arange(pairs.shape[0]), pairs.shape[0] // 11)
+    order = np.concatenate([runs[k] for k in np.random.default_rng(23).permutation(len(runs))])
+    pairs, wpair = pairs[order], wpair[order]
+    exp = oracle.routed(pairs, ref, qer, wpair, DEFAULT, bits=0, nthreads=8)
+    with _bsw(DEFAULT) as bsw:
+        got = pairs.copy()
+        bsw.scores_batched(got, ref, qer, got.shape[0], w=16, wpair=wpair, bits=0)
+        flagged, groups = bsw.last_regroup()
+    _assert_same(exp, got, "batched form, mixed extension batches")
+    assert flagged >= 1 and groups >= 1
 
 
 @pytest.mark.parametrize("wl,bits,n", [(synth.C2, 16, 3000), (synth.C1_8, 8, 5001), (synth.C4, 16, 70)])
