@@ -121,14 +121,11 @@ __device__ __forceinline__ void lane_group4(uint32_t *hp, int j, uint32_t w0, ui
     hp[32] = __byte_perm((uint32_t)H[0], (uint32_t)f2[1], 0x5410u);
     hp[64] = __byte_perm((uint32_t)H[1], (uint32_t)f2[2], 0x5410u);
     hp[96] = __byte_perm((uint32_t)H[2], (uint32_t)f2[3], 0x5410u);
-    const uint32_t k0 = __byte_perm((uint32_t)(j + 1), (uint32_t)H[0], 0x5410u);
-    const uint32_t k1 = __byte_perm((uint32_t)(j + 2), (uint32_t)H[1], 0x5410u);
-    const uint32_t k2 = __byte_perm((uint32_t)(j + 3), (uint32_t)H[2], 0x5410u);
-    const uint32_t k3 = __byte_perm((uint32_t)(j + 4), (uint32_t)H[3], 0x5410u);
-    const uint32_t ka = k0 > k1 ? k0 : k1;
-    const uint32_t kb = k2 > k3 ? k2 : k3;
-    const uint32_t kc = ka > kb ? ka : kb;
-    key = kc > key ? kc : key;
+    // the row-max key takes the group's maximum with one past its last
+    // column; the row's end resolves it to the last column holding it
+    const int m4 = __vimax3_s32(H[0], H[1], imax(H[2], H[3]));
+    const uint32_t kg = __byte_perm((uint32_t)(j + 4), (uint32_t)m4, 0x5410u);
+    key = kg > key ? kg : key;
     hprev = H[3];
 }
 
@@ -503,8 +500,19 @@ __global__ void __launch_bounds__(128) bsw_lane_kernel(LaunchArgs A) {
             s.gscore = imax(s.gscore, hprev);
         }
         const int maxRS1 = (int)(key >> 16);
-        const int y1 = (int)(key & 0xffffu);
         if (maxRS1 == 0) { finish(); continue; }  // a zero row ends the pair (:3206-3211)
+        // y1 = one past the last column holding the row maximum.  A key is one
+        // past a single column (which holds the maximum) or one past a group of
+        // four (the last of them that holds it); the row's H(c) of a column
+        // scored in the clean middle is stored at column c + 1.
+        int y1;
+        {
+            const int k = (int)(key & 0xffffu);
+            const int a3 = (int)(hf(k) & 0xffffu);
+            const int a2 = (int)(hf(imax(k - 1, 0)) & 0xffffu);
+            const int a1 = (int)(hf(imax(k - 2, 0)) & 0xffffu);
+            y1 = a3 == maxRS1 ? k : a2 == maxRS1 ? k - 1 : a1 == maxRS1 ? k - 2 : k - 3;
+        }
         {   // maximum, its position and max_off (:3213-3226)
             const int bmax = s.maxScore;
             s.maxScore = imax(s.maxScore, maxRS1);
