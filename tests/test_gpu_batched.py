@@ -64,3 +64,24 @@ def test_batched_golden_edges():
         with _bsw(P) as bsw:
             bsw.scores_batched(got, d["ref"], d["qer"], got.shape[0], int(d["w"]), bits=16)
         _same(d["expected"], got, os.path.basename(f))
+
+
+@pytest.mark.parametrize("field,k", [("len2", 0), ("idr", 777), ("len1", 1998)])
+def test_batched_host_call_refuses_negative_lengths_and_offsets(field, k):
+    """The host call reduces its sequence extents on the device and refuses a
+    pair with a negative length or offset: TAL_EDOMAIN naming the first such
+    pair; the same handle then scores a good batch."""
+    wl = synth.C3
+    b = synth.generate(wl, 2000)
+    P = wl.params()
+    bad = b.pairs.copy()
+    bad[field][k] = -3
+    bad["idq"][k + 1] = -1  # a later one: the first is reported
+    with _bsw(P) as bsw:
+        with pytest.raises(tal_bsw.TalBswError) as ei:
+            bsw.scores_batched(bad, b.ref, b.qer, b.n, 100, wpair=b.w, bits=tal_bsw.AUTO)
+        assert ei.value.status == tal_bsw.api.TAL_EDOMAIN and ei.value.bad_pair == k
+        got = b.pairs.copy()
+        bsw.scores_batched(got, b.ref, b.qer, b.n, 100, wpair=b.w, bits=tal_bsw.AUTO)
+    exp = oracle.routed(b.pairs, b.ref, b.qer, b.w, P, bits=0, nthreads=4)
+    _same(exp, got, "batched c3 after a refusal")

@@ -351,6 +351,38 @@ using namespace talbsw;
 
 namespace {
 
+// Byte extents of the sequence buffers a device SeqPair array references
+// (out[0]: max idr + len1, out[1]: max idq + len2) and its first pair with a
+// negative length or offset (out[2]: n - its index; 0 if none), all by
+// atomicMax into a zeroed out[3].
+__global__ void extent_kernel(const talbsw::DevPair *p, int n, unsigned long long *out) {
+    unsigned long long r = 0, q = 0, bad = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const talbsw::DevPair x = p[k];
+        if (x.len1 < 0 || x.len2 < 0 || x.idr < 0 || x.idq < 0) {
+            bad = bad > (unsigned long long)(n - k) ? bad : (unsigned long long)(n - k);
+        } else {
+            const unsigned long long re = (unsigned long long)x.idr + (unsigned long long)x.len1;
+            const unsigned long long qe = (unsigned long long)x.idq + (unsigned long long)x.len2;
+            r = r > re ? r : re;
+            q = q > qe ? q : qe;
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long r2 = __shfl_xor_sync(0xffffffffu, r, o);
+        const unsigned long long q2 = __shfl_xor_sync(0xffffffffu, q, o);
+        const unsigned long long b2 = __shfl_xor_sync(0xffffffffu, bad, o);
+        r = r > r2 ? r : r2;
+        q = q > q2 ? q : q2;
+        bad = bad > b2 ? bad : b2;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out + 0, r);
+        atomicMax(out + 1, q);
+        if (bad) atomicMax(out + 2, bad);
+    }
+}
+
 int bfail(tal_bsw_ctx *h, int code, const std::string &msg) {
     h->last_error = msg;
     return code;
@@ -572,25 +604,38 @@ int tal_bsw_scores_batched(tal_bsw_handle h, tal_seq_pair *pairs, const uint8_t 
     if (!pairs || !seqBufRef || !seqBufQer) return bfail(h, TAL_EINVAL, "NULL buffer");
     cudaError_t e = cudaSetDevice(h->device);
     if (e != cudaSuccess) return bfail(h, TAL_ECUDA, "cudaSetDevice");
-    long long rhi = 16, qhi = 16;
-    for (int32_t k = 0; k < numPairs; k++) {
-        const tal_seq_pair &p = pairs[k];
-        if (p.len1 < 0 || p.len2 < 0 || p.idr < 0 || p.idq < 0) {
-            h->last_bad = k;
-            return bfail(h, TAL_EDOMAIN, "negative length or offset at pair " + std::to_string(k));
-        }
-        rhi = std::max<long long>(rhi, (long long)p.idr + p.len1);
-        qhi = std::max<long long>(qhi, (long long)p.idq + p.len2);
-    }
+    // the pairs first; the extents of the sequence buffers they reference
+    // (and the first pair with a negative length or offset) are reduced on
+    // the device, not by a pass of the host over the array
     const size_t pbytes = (size_t)numPairs * sizeof(tal_seq_pair);
-    if ((e = h->pairs.ensure(pbytes)) != cudaSuccess ||
-        (e = h->ref.ensure((size_t)rhi + 16)) != cudaSuccess ||
+    if ((e = h->pairs.ensure(pbytes)) != cudaSuccess || (e = h->caps.ensure(4 * sizeof(unsigned long long))) != cudaSuccess)
+        return bfail(h, TAL_ENOMEM, std::string("device buffers: ") + cudaGetErrorString(e));
+    unsigned long long *ext = reinterpret_cast<unsigned long long *>(h->caps.p);
+    e = cudaMemcpyAsync(h->pairs.p, pairs, pbytes, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ext, 0, 3 * sizeof(unsigned long long), h->stream);
+    if (e == cudaSuccess) {
+        const int blocks = (int)std::min<long long>(((long long)numPairs + 255) / 256, (long long)h->num_sms * 8);
+        extent_kernel<<<blocks, 256, 0, h->stream>>>(reinterpret_cast<const talbsw::DevPair *>(h->pairs.p),
+                                                     numPairs, ext);
+        h->launches++;
+        e = cudaGetLastError();
+    }
+    unsigned long long hext[3] = {0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hext, ext, sizeof(hext), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return bfail(h, TAL_ECUDA, std::string("H2D: ") + cudaGetErrorString(e));
+    if (hext[2]) {
+        const long long k = (long long)numPairs - (long long)hext[2];
+        h->last_bad = k;
+        return bfail(h, TAL_EDOMAIN, "negative length or offset at pair " + std::to_string(k));
+    }
+    const long long rhi = std::max<long long>(16, (long long)hext[0]);
+    const long long qhi = std::max<long long>(16, (long long)hext[1]);
+    if ((e = h->ref.ensure((size_t)rhi + 16)) != cudaSuccess ||
         (e = h->qer.ensure((size_t)qhi + 16)) != cudaSuccess ||
         (wpair && (e = h->wpair.ensure(sizeof(int32_t) * (size_t)numPairs)) != cudaSuccess))
         return bfail(h, TAL_ENOMEM, std::string("device buffers: ") + cudaGetErrorString(e));
-    e = cudaMemcpyAsync(h->pairs.p, pairs, pbytes, cudaMemcpyHostToDevice, h->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(h->ref.p, seqBufRef, (size_t)rhi, cudaMemcpyHostToDevice, h->stream);
+    e = cudaMemcpyAsync(h->ref.p, seqBufRef, (size_t)rhi, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h->qer.p, seqBufQer, (size_t)qhi, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess && wpair)
