@@ -31,6 +31,13 @@ import sys
 import tempfile
 import time
 
+# The batched form and the serving ticks run their segment launches on up to
+# 32 forked streams; with CUDA's default of 8 hardware work queues, streams
+# that share a queue serialise their launches (a 200,000-pair tick's short
+# segments start only after the long ones).  Set before the CUDA context
+# exists; an explicit setting in the environment wins.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "trans-omics-acceleration-library_gb300")
 for _p in (ROOT, PKG):
@@ -478,6 +485,7 @@ def run_ours(args):
                    "ref_cells_per_step": int(total_cells), "kernel_cells_per_step": int(kernel_cells) * ws,
                    "call": "tal_bsw_scores_batched_device (device-resident), one CUDA graph per call",
                    "l2": "inputs larger than L2 (no flush needed)",
+                   "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                    "parallelism": f"replica shards x{ws}, no collective"},
         "pairs_per_s": round(total_pairs / t_step_max, 1),
         "wall_s_timed": round(wall, 3),

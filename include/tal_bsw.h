@@ -316,7 +316,10 @@ int64_t tal_bsw_now_ns(void);
 
 /* Creates a server with the scoring parameters of `h` and its length-bin
  * configurations (the autotuner's, when h ran a batched call; else the
- * defaults), on h's device.  h may be destroyed afterwards. */
+ * defaults), on h's device.  h may be destroyed afterwards.  A tick's
+ * segment launches run on up to 32 streams: start the process with
+ * CUDA_DEVICE_MAX_CONNECTIONS=32 so they do not share CUDA's default 8
+ * hardware queues (the same holds for tal_bsw_scores_batched). */
 int tal_bsw_server_create(tal_bsw_handle h, const tal_bsw_server_config *cfg,
                           tal_bsw_server_handle *out);
 
