@@ -294,10 +294,13 @@ cudaError_t enqueue_segs_forked(tal_bsw_ctx *h, const SortBufs &sb, const Launch
     }
     cudaError_t e = cudaEventRecord(f.fork, s);
     bool used[kForkStreams] = {};
+    int nz = 0;  // non-empty segments so far
     for (int sg = 0; sg < kNumSegs && e == cudaSuccess; sg++) {  // longest queries first
         const int ns = count ? count[sg] : n;
         if (ns <= 0) continue;
-        const int k = sg % kForkStreams;
+        const int k = cap != cudaStreamCaptureStatusNone ? sg % kForkStreams
+                      : nz < kForkStreams ? nz : kForkStreams - 1 - (nz - kForkStreams) % kForkStreams;
+        nz++;
         if (!used[k]) {
             e = cudaStreamWaitEvent(f.st[k], f.fork, 0);
             used[k] = true;
