@@ -67,6 +67,9 @@ def parse_args():
     ap.add_argument("--profile-call", action="store_true",
                     help="profiling: warm up the batched call (--warmup calls), print the library's "
                          "launch counter, make one more call and exit (no timing, no JSON line)")
+    ap.add_argument("--trace-tick", type=int, default=0,
+                    help="serve single requests of this many c3_mixed pairs, one at a time, with the "
+                         "library's segment trace on (stderr), and print each tick's time (profiling)")
     ap.add_argument("--profile-plain", action="store_true",
                     help="with --profile-call: the plain launch (tal_bsw_scores_device) instead of the batched form")
     ap.add_argument("--no-grouped", action="store_true",
@@ -1078,12 +1081,59 @@ def profile_call(args):
     bsw.close()
 
 
+def trace_tick(args):
+    """Single serving requests of --trace-tick C3 pairs, each alone in its tick,
+    with TAL_BSW_TRACE=1: the library prints each segment launch's start / end
+    (ms after the tick's fork; it synchronises the tick after its segments, so
+    the request's launch-to-done time printed here is what follows them -- the
+    regroup pass and the copies back)."""
+    os.environ["TAL_BSW_TRACE"] = "1"
+    import torch
+    import tal_bsw
+    from tal_bsw import synth
+    from tal_bsw.api import BswServer
+    n = args.trace_tick
+    wl = synth.C3
+    npool = max(3 * n, 1_000_000)
+    b = synth.generate(wl, npool, first=20_000_000)
+    P = wl.params()
+    bsw = tal_bsw.BandedPairWiseSW(P["o_del"], P["e_del"], P["o_ins"], P["e_ins"], P["zdrop"],
+                                   P["end_bonus"], None, P["a"], P["b"], 1, device=0)
+    tmp = b.pairs.copy()
+    bsw.scores_batched(tmp, b.ref, b.qer, npool, 100, wpair=b.w, bits=tal_bsw.AUTO)  # autotune
+
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        v = t.numpy().view(a.dtype).reshape(a.shape)
+        v[...] = a
+        return v, t
+    hp, _hp = pinned(b.pairs)
+    hr, _hr = pinned(b.ref)
+    hq, _hq = pinned(b.qer)
+    hw, _hw = pinned(b.w.astype(np.int32))
+    srv = BswServer(bsw)
+    for k in range(args.warmup + args.steps):
+        lo = (k * n) % (npool - n + 1)
+        t = srv.submit(hp[lo:lo + n], hr, hq, w=100, wpair=hw[lo:lo + n], bits=tal_bsw.AUTO)
+        info = srv.poll(t, timeout_us=60_000_000)
+        assert info is not None and info.status == 0
+        if k >= args.warmup:
+            sub = b.pairs[lo:lo + n]
+            print(f"tick {k - args.warmup}: pairs {lo}..{lo + n}, max len2 {int(sub['len2'].max())}, "
+                  f"launch -> done after the segments {(info.done_ns - info.launch_ns) / 1e6:.2f} ms",
+                  file=sys.stderr, flush=True)
+    srv.close()
+    bsw.close()
+
+
 def main():
     import faulthandler
     faulthandler.enable()
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.trace_tick:
+        trace_tick(args)
     elif args.profile_call:
         profile_call(args)
     else:
