@@ -149,3 +149,17 @@ def test_serving_bad_pair_fails_only_its_request(c3):
     _same(exp[2000:3000], got[2000:3000], "request after the bad one")
     keep = np.r_[1000:bad_pair, bad_pair + 1:2000]
     _same(exp[keep], got[keep], "good pairs of the bad request")
+
+
+def test_serving_one_large_tick_is_exact(c3):
+    """A tick run like the batched form (one launch per non-empty segment, each
+    on its own stream while they last, the shortest-query ones queued behind
+    the shortest before them): every segment of the C3 mix in one request, and
+    the outputs equal the reference's."""
+    wl, b, P, exp = c3
+    with _bsw(P) as bsw, tal_bsw.BswServer(bsw, pool_bytes=1 << 30, latency_pairs=-1) as srv:
+        got = b.pairs.copy()
+        t = srv.submit(got, b.ref, b.qer, w=100, wpair=b.w, bits=0)
+        info = _wait(srv, t)
+        assert info.status == TAL_OK and info.tick_requests == 1
+    _same(exp, got, "one large tick")
